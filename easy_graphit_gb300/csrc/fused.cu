@@ -1,0 +1,310 @@
+// Whole-loop persistent kernels: the fuse_kernel(true, ...) form of the BFS and
+// SSSP loops (src/graphit/operators.cpp:652-672, gpu_intrinsics.h:113-117).
+// One cooperatively launched grid (all CTAs co-resident) runs every iteration;
+// the LB functions of lb.cuh process virtual CTAs, and a bounded grid barrier
+// (common.cuh) separates iterations.  Frontier sizes never leave the device.
+//
+// Sparse-queue counts rotate through three slots: iteration L reads slot
+// (L-1)%3, appends to slot L%3 and clears slot (L+1)%3, whose last reader
+// finished before the previous barrier -- one barrier per iteration.
+#include <cstdlib>
+
+#include "engine.h"
+#include "lb.cuh"
+#include "udf.cuh"
+
+namespace gg {
+
+uint64_t barrier_timeout_ns() {
+  static uint64_t t = [] {
+    const char *e = getenv("GG_BARRIER_TIMEOUT_MS");
+    const long ms = e ? atol(e) : 0;
+    return (uint64_t)(ms > 0 ? ms : 30000) * 1000000ull;
+  }();
+  return t;
+}
+
+bool fused_supported(const gg_schedule *s) {
+  if (s->direction != GG_PUSH || s->frontier_creation != GG_FC_SPARSE) return false;
+  switch (s->load_balancing) {
+    case GG_LB_VERTEX_BASED:
+    case GG_LB_WM:
+    case GG_LB_TWCE:
+    case GG_LB_CM:
+      return true;
+    default:
+      return false;
+  }
+}
+
+template <int LB, class F>
+__device__ __forceinline__ void run_lb(const DGraph &g, const Enum &en, int32_t n, const F &f,
+                                       const DOut &out, int4 *smem) {
+  if (LB == GG_LB_VERTEX_BASED) {
+    const int32_t nv = ceil_div(n, blockDim.x);
+    for (int32_t v = blockIdx.x; v < nv; v += gridDim.x) lb_vertex(g, en, n, f, out, v);
+  } else if (LB == GG_LB_WM) {
+    const int32_t nv = ceil_div(n, blockDim.x >> 5);
+    for (int32_t v = blockIdx.x; v < nv; v += gridDim.x) lb_wm(g, en, n, f, out, v);
+  } else if (LB == GG_LB_TWCE) {
+    const int32_t nv = ceil_div(n, blockDim.x / kStage1);
+    for (int32_t v = blockIdx.x; v < nv; v += gridDim.x)
+      lb_twce<F, true>(g, en, n, f, out, v, *reinterpret_cast<TwceSmem *>(smem));
+  } else {
+    const int32_t nv = ceil_div(n, blockDim.x);
+    for (int32_t v = blockIdx.x; v < nv; v += gridDim.x)
+      lb_cm(g, en, n, f, out, v, *reinterpret_cast<CmSmem *>(smem));
+  }
+}
+
+struct FusedArgs {
+  DGraph g;
+  int32_t *q0, *q1;
+  int32_t *cnt3;  // rotating counts [3]
+  int64_t cap;
+  uint32_t *bar;
+  int32_t *err;
+  uint64_t timeout_ns;
+  int32_t *stats;  // [0] iterations, [1] bucket advances
+  VData vd;
+  int32_t delta;
+  int32_t *gmin2;  // SSSP bucket-advance minima [2]
+};
+
+__device__ __forceinline__ DOut sparse_out(const FusedArgs &a, int32_t *q, int64_t it) {
+  DOut o{};
+  o.mode = OUT_SPARSE;
+  o.q = q;
+  o.cnt = a.cnt3 + it % 3;
+  o.cap = a.cap;
+  o.err = a.err;
+  return o;
+}
+
+template <int LB>
+__global__ void __launch_bounds__(1024) k_bfs_fused(FusedArgs a) {
+  extern __shared__ int4 smem[];
+  int32_t *qs[2] = {a.q0, a.q1};
+  int in = 0;
+  int64_t level = 1;
+  for (;; ++level) {
+    const int32_t n = *(volatile int32_t *)(a.cnt3 + (level - 1) % 3);
+    if (n == 0 || *(volatile int32_t *)a.err) break;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.cnt3[(level + 1) % 3] = 0;
+    const Enum en{qs[in], nullptr, n};
+    const EdgeF<UBfs, false> f{UBfs{a.vd.parent, a.vd.depth, (int32_t)level},
+                               DIn{IN_ALL, nullptr, nullptr}, DIn{IN_ALL, nullptr, nullptr}, true};
+    run_lb<LB>(a.g, en, n, f, sparse_out(a, qs[in ^ 1], level), smem);
+    if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
+    in ^= 1;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.stats[0] = (int32_t)(level - 1);
+}
+
+// Delta-stepping with the GPUPriorityQueue semantics of gpu_priority_queue.h:
+// relax the frontier with cutoff cur+delta; when it runs empty, advance cur to
+// the smallest priority >= cur+delta and enqueue [cur, cur+delta).
+template <int LB>
+__global__ void __launch_bounds__(1024) k_sssp_fused(FusedArgs a) {
+  extern __shared__ int4 smem[];
+  __shared__ int32_t wmin[32];
+  int32_t *qs[2] = {a.q0, a.q1};
+  const int32_t V = a.g.V;
+  int in = 0;
+  int64_t it = 1, cur = 0, adv = 0, relax = 0;
+  for (;; ++it) {
+    const int32_t n = *(volatile int32_t *)(a.cnt3 + (it - 1) % 3);
+    if (*(volatile int32_t *)a.err) break;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.cnt3[(it + 1) % 3] = 0;
+    if (n == 0) {
+      const int64_t window = cur + a.delta;
+      int32_t *gm = a.gmin2 + (adv & 1);
+      if (blockIdx.x == 0 && threadIdx.x == 0) a.gmin2[(adv + 1) & 1] = INT_MAX;
+      int32_t m = INT_MAX;
+      if (window < INT_MAX)
+        for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+          const int32_t p = a.vd.dist[v];
+          if (p >= window && p != INT_MAX && p < m) m = p;
+        }
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, d));
+      if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = m;
+      __syncthreads();
+      if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x >> 5) ? wmin[threadIdx.x] : INT_MAX;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, d));
+        if (threadIdx.x == 0 && m != INT_MAX) atomicMin(gm, m);
+      }
+      if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
+      cur = *(volatile int32_t *)gm;
+      ++adv;
+      if (cur == INT_MAX) break;
+      const int64_t hi = cur + a.delta;
+      int32_t *qo = qs[in ^ 1];
+      int32_t *cnt = a.cnt3 + it % 3;
+      const int32_t stride = gridDim.x * blockDim.x;
+      for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < ceil_div(V, stride) * stride;
+           v += stride) {
+        bool p = false;
+        if (v < V) {
+          const int32_t x = a.vd.dist[v];
+          p = x >= cur && (int64_t)x < hi;
+        }
+        const uint32_t mk = __ballot_sync(0xffffffffu, p);
+        if (mk) {
+          const int32_t lane = threadIdx.x & 31;
+          int32_t base = 0;
+          if (lane == 0) base = atomicAdd(cnt, __popc(mk));
+          base = __shfl_sync(0xffffffffu, base, 0);
+          if (p) qo[base + __popc(mk & ((1u << lane) - 1))] = v;
+        }
+      }
+    } else {
+      const int64_t c = cur + a.delta;
+      const Enum en{qs[in], nullptr, n};
+      const EdgeF<USssp, false> f{USssp{a.vd.dist, c > INT_MAX ? INT_MAX : (int32_t)c},
+                                  DIn{IN_ALL, nullptr, nullptr}, DIn{IN_ALL, nullptr, nullptr}, false};
+      run_lb<LB>(a.g, en, n, f, sparse_out(a, qs[in ^ 1], it), smem);
+      ++relax;
+    }
+    if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
+    in ^= 1;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.stats[0] = (int32_t)relax;
+    a.stats[1] = (int32_t)adv;
+  }
+}
+
+template <class K>
+static gg_status coop_launch(gg_graph *g, K kernel, int cta, size_t smem, FusedArgs &a) {
+  int per_sm = 0;
+  if (smem > 48 * 1024)
+    GG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, cta, smem));
+  if (per_sm < 1) return set_error(GG_ERR_UNSUPPORTED, "fused kernel does not fit on an SM");
+  const int grid = per_sm * g->sm_count;
+  GG_CUDA(cudaMemsetAsync(g->d_bar, 0, sizeof(uint32_t) * 2, g->stream));
+  void *args[] = {&a};
+  GG_CUDA(cudaLaunchCooperativeKernel((const void *)kernel, grid, cta, args, smem, g->stream));
+  return GG_OK;
+}
+
+static size_t lb_smem(int lb, int cta) {
+  if (lb == GG_LB_TWCE) return twce_smem_bytes(cta);
+  if (lb == GG_LB_CM) return cm_smem_bytes(cta);
+  return 0;
+}
+
+static FusedArgs make_args(gg_graph *g, gg_frontier *f, const VData &vd) {
+  FusedArgs a{};
+  a.g = g->csr.view();
+  a.g.nbuckets = 0;
+  a.q0 = f->q_in;
+  a.q1 = f->q_out;
+  a.cnt3 = g->d_misc + 40;
+  a.cap = f->cap;
+  a.bar = g->d_bar;
+  a.err = g->d_err;
+  a.timeout_ns = barrier_timeout_ns();
+  a.stats = g->d_misc + 44;
+  a.vd = vd;
+  a.gmin2 = g->d_misc + 46;
+  return a;
+}
+
+// Counts start as {1 (the source), 0, 0}; both minima slots at INT_MAX.
+static gg_status init_counts(gg_graph *g) {
+  int32_t *h = g->h_pinned + 40;
+  h[0] = 1;
+  h[1] = 0;
+  h[2] = 0;
+  h[3] = 0;
+  h[4] = 0;
+  h[5] = 0;
+  h[6] = INT_MAX;
+  h[7] = INT_MAX;
+  GG_CUDA(cudaMemcpyAsync(g->d_misc + 40, h, sizeof(int32_t) * 8, cudaMemcpyHostToDevice, g->stream));
+  return GG_OK;
+}
+
+static gg_status read_stats(gg_graph *g, int32_t *iters, int64_t *adv) {
+  GG_CUDA(cudaMemcpyAsync(g->h_pinned + 50, g->d_misc + 44, sizeof(int32_t) * 2, cudaMemcpyDeviceToHost,
+                          g->stream));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  *iters = g->h_pinned[50];
+  if (adv) *adv = g->h_pinned[51];
+  return GG_OK;
+}
+
+gg_status fused_bfs(gg_graph *g, const gg_schedule *s, int32_t, const VData &vd, gg_frontier *f,
+                    int32_t *iters, bool *ran) {
+  *ran = false;
+  if (!fused_supported(s)) return GG_OK;
+  GG_TRY(init_counts(g));
+  FusedArgs a = make_args(g, f, vd);
+  const int cta = s->cta_size;
+  const size_t sm = lb_smem(s->load_balancing, cta);
+  switch (s->load_balancing) {
+    case GG_LB_VERTEX_BASED: GG_TRY(coop_launch(g, k_bfs_fused<GG_LB_VERTEX_BASED>, cta, sm, a)); break;
+    case GG_LB_WM: GG_TRY(coop_launch(g, k_bfs_fused<GG_LB_WM>, cta, sm, a)); break;
+    case GG_LB_TWCE: GG_TRY(coop_launch(g, k_bfs_fused<GG_LB_TWCE>, cta, sm, a)); break;
+    default: GG_TRY(coop_launch(g, k_bfs_fused<GG_LB_CM>, cta, sm, a)); break;
+  }
+  GG_TRY(read_stats(g, iters, nullptr));
+  *ran = true;
+  return GG_OK;
+}
+
+gg_status fused_sssp(gg_graph *g, const gg_schedule *s, int32_t, int32_t delta, const VData &vd,
+                     gg_frontier *f, int32_t *iters, int64_t *advances, bool *ran) {
+  *ran = false;
+  if (!fused_supported(s)) return GG_OK;
+  GG_TRY(init_counts(g));
+  FusedArgs a = make_args(g, f, vd);
+  a.delta = delta;
+  const int cta = s->cta_size;
+  const size_t sm = lb_smem(s->load_balancing, cta);
+  switch (s->load_balancing) {
+    case GG_LB_VERTEX_BASED: GG_TRY(coop_launch(g, k_sssp_fused<GG_LB_VERTEX_BASED>, cta, sm, a)); break;
+    case GG_LB_WM: GG_TRY(coop_launch(g, k_sssp_fused<GG_LB_WM>, cta, sm, a)); break;
+    case GG_LB_TWCE: GG_TRY(coop_launch(g, k_sssp_fused<GG_LB_TWCE>, cta, sm, a)); break;
+    default: GG_TRY(coop_launch(g, k_sssp_fused<GG_LB_CM>, cta, sm, a)); break;
+  }
+  GG_TRY(read_stats(g, iters, advances));
+  *ran = true;
+  return GG_OK;
+}
+
+// A barrier that waits for one block more than were launched: it can only end
+// by its time limit.
+__global__ void k_barrier_never(uint32_t *bar, int32_t *err, uint64_t timeout_ns) {
+  grid_barrier(bar, gridDim.x + 1, err, timeout_ns);
+}
+
+}  // namespace gg
+
+using namespace gg;
+
+extern "C" gg_status gg_debug_barrier_timeout(int32_t timeout_us) {
+  GG_CHECK_ARG(timeout_us > 0 && timeout_us <= 10 * 1000 * 1000, "timeout must be in (0, 10 s]");
+  uint32_t *bar = nullptr;
+  int32_t *err = nullptr;
+  GG_CUDA(cudaMalloc(&bar, sizeof(uint32_t) * 2));
+  GG_CUDA(cudaMalloc(&err, sizeof(int32_t)));
+  GG_CUDA(cudaMemset(bar, 0, sizeof(uint32_t) * 2));
+  GG_CUDA(cudaMemset(err, 0, sizeof(int32_t)));
+  k_barrier_never<<<2, 32>>>(bar, err, (uint64_t)timeout_us * 1000ull);
+  cudaError_t le = cudaGetLastError();
+  cudaError_t se = cudaDeviceSynchronize();
+  int32_t h = 0;
+  cudaMemcpy(&h, err, sizeof(int32_t), cudaMemcpyDeviceToHost);
+  cudaFree(bar);
+  cudaFree(err);
+  if (le != cudaSuccess || se != cudaSuccess)
+    return set_error(GG_ERR_CUDA, "barrier probe launch failed: %s",
+                     cudaGetErrorString(le != cudaSuccess ? le : se));
+  if (h & DEV_ERR_TIMEOUT) return set_error(GG_ERR_TIMEOUT, "grid barrier wait timed out as designed");
+  return GG_OK;
+}

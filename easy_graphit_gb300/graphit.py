@@ -1,0 +1,462 @@
+"""Python mirror of the GraphIt GPU algorithm and scheduling API.
+
+Names follow easy_graphit's `include/graphit/schedule.h` (SimpleGPUSchedule,
+HybridGPUSchedule and their enums/config methods), `include/graphit/operators.h`
+(edgeset_apply(...).from_(...).to(...).apply / apply_modified / apply_priority,
+vertexset_apply) and the runtime objects of `runtime/infra_gpu/` (GraphT,
+VertexFrontier, GPUPriorityQueue, VertexFrontierList).  Everything executes in
+libgg.so on the GPU; this module only marshals arguments.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from enum import IntEnum
+from typing import Optional
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import call, lib
+
+
+# --------------------------------------------------------------- schedules
+class SimpleGPUSchedule:
+    """graphit::SimpleGPUSchedule (schedule.h:26-118)."""
+
+    default_max_cta = 60   # schedule.cpp:6
+    default_cta_size = 512  # schedule.cpp:5
+
+    class direction_type(IntEnum):
+        PUSH = 0
+        PULL = 1
+
+    class pull_frontier_rep_type(IntEnum):
+        BITMAP = 0
+        BOOLMAP = 1
+
+    class frontier_creation_type(IntEnum):
+        SPARSE = 0
+        BITMAP = 1
+        BOOLMAP = 2
+
+    class deduplication_type(IntEnum):
+        DISABLED = 0
+        ENABLED = 1
+
+    class deduplication_strategy_type(IntEnum):
+        FUSED = 0
+        UNFUSED = 1
+
+    class load_balancing_type(IntEnum):
+        VERTEX_BASED = 0
+        TWC = 1
+        TWCE = 2
+        WM = 3
+        CM = 4
+        STRICT = 5
+        EDGE_ONLY = 6
+        ETWC = 7  # not in the reference enum
+
+    class edge_blocking_type(IntEnum):
+        BLOCKED = 0
+        UNBLOCKED = 1
+
+    class kernel_fusion_type(IntEnum):
+        DISABLED = 0
+        ENABLED = 1
+
+    def __init__(self):
+        T = SimpleGPUSchedule
+        self.direction = T.direction_type.PUSH
+        self.load_balancing = T.load_balancing_type.VERTEX_BASED
+        self.edge_blocking = T.edge_blocking_type.UNBLOCKED
+        self.frontier_creation = T.frontier_creation_type.SPARSE
+        self.pull_frontier_rep = T.pull_frontier_rep_type.BOOLMAP
+        self.deduplication = T.deduplication_type.DISABLED
+        self.deduplication_strategy = T.deduplication_strategy_type.FUSED
+        self.kernel_fusion = T.kernel_fusion_type.DISABLED
+        self.block_size = -1
+        self.max_cta = T.default_max_cta
+        self.cta_size = T.default_cta_size
+
+    def configDirection(self, dir, pf=None):
+        self.direction = SimpleGPUSchedule.direction_type(dir)
+        if self.direction == SimpleGPUSchedule.direction_type.PULL:
+            self.pull_frontier_rep = SimpleGPUSchedule.pull_frontier_rep_type(
+                SimpleGPUSchedule.pull_frontier_rep_type.BOOLMAP if pf is None else pf)
+        return self
+
+    def configFrontierCreation(self, fc):
+        self.frontier_creation = SimpleGPUSchedule.frontier_creation_type(fc)
+        return self
+
+    def configDeduplication(self, dedup, strategy=None):
+        self.deduplication = SimpleGPUSchedule.deduplication_type(dedup)
+        if strategy is not None:
+            self.deduplication_strategy = SimpleGPUSchedule.deduplication_strategy_type(strategy)
+        return self
+
+    def configLoadBalancing(self, lb, eb=None, bs=-1):
+        self.load_balancing = SimpleGPUSchedule.load_balancing_type(lb)
+        if self.load_balancing == SimpleGPUSchedule.load_balancing_type.EDGE_ONLY:
+            self.edge_blocking = SimpleGPUSchedule.edge_blocking_type(
+                SimpleGPUSchedule.edge_blocking_type.UNBLOCKED if eb is None else eb)
+            self.block_size = bs
+        return self
+
+    def configKernelFusion(self, kf):
+        self.kernel_fusion = SimpleGPUSchedule.kernel_fusion_type(kf)
+        return self
+
+    def to_c(self) -> L.gg_schedule:
+        return L.gg_schedule(int(self.direction), int(self.pull_frontier_rep),
+                             int(self.frontier_creation), int(self.deduplication),
+                             int(self.deduplication_strategy), int(self.load_balancing),
+                             int(self.edge_blocking), int(self.block_size),
+                             int(self.kernel_fusion), int(self.max_cta), int(self.cta_size))
+
+    def __repr__(self):
+        return (f"SimpleGPUSchedule({self.direction.name}, {self.load_balancing.name}, "
+                f"creation={self.frontier_creation.name}, pull_rep={self.pull_frontier_rep.name}, "
+                f"blocking={self.edge_blocking.name}:{self.block_size}, cta={self.cta_size})")
+
+
+class HybridGPUSchedule:
+    """graphit::HybridGPUSchedule (schedule.h:122-139): s1 when
+    |frontier| <= threshold * V, else s2 (operators.cpp:526)."""
+
+    def __init__(self, s1: SimpleGPUSchedule, s2: SimpleGPUSchedule):
+        self.s1, self.s2 = s1, s2
+        self.threshold = 0.0
+
+    def configThreshold(self, t: float):
+        self.threshold = float(t)
+        return self
+
+    def bindThreshold(self, t: float):  # the runtime-bound threshold of schedule.cpp:9-12
+        self.threshold = float(t)
+        return self
+
+
+D, LB, FC, PR_ = (SimpleGPUSchedule.direction_type, SimpleGPUSchedule.load_balancing_type,
+                  SimpleGPUSchedule.frontier_creation_type, SimpleGPUSchedule.pull_frontier_rep_type)
+
+
+def app_schedule(s, fuse: bool = False) -> L.gg_app_schedule:
+    a = L.gg_app_schedule()
+    a.fuse = int(bool(fuse))
+    if isinstance(s, HybridGPUSchedule):
+        a.kind = 1
+        a.s1, a.s2, a.threshold = s.s1.to_c(), s.s2.to_c(), s.threshold
+    else:
+        s = s or SimpleGPUSchedule()
+        a.kind = 0
+        a.s1 = s.to_c()
+        a.s2 = s.to_c()
+    return a
+
+
+def default_schedule(app: str, power: bool = False, threshold: float = 0.12):
+    """The schedules chosen in each app's main() (apps/*.cpp) as
+    (schedule, fuse).  `power` selects the alternative ("power") schedule."""
+    def s():
+        return SimpleGPUSchedule()
+    if app == "bfs":  # bfs.cpp:69-92
+        if power:
+            s1 = s().configDirection(D.PUSH).configLoadBalancing(LB.TWCE)
+            s2 = (s().configDirection(D.PULL, PR_.BITMAP).configLoadBalancing(LB.VERTEX_BASED)
+                  .configFrontierCreation(FC.BITMAP))
+            return HybridGPUSchedule(s1, s2).bindThreshold(threshold), False
+        return s().configDirection(D.PUSH).configLoadBalancing(LB.TWCE), True
+    if app == "sssp":  # sssp.cpp:65-83
+        if power:
+            return (s().configDirection(D.PUSH).configLoadBalancing(LB.TWCE)
+                    .configFrontierCreation(FC.BOOLMAP)), False
+        return s().configDirection(D.PUSH).configFrontierCreation(FC.SPARSE), True
+    if app == "pr":  # pr.cpp:79-81
+        return (s().configDirection(D.PULL).configLoadBalancing(
+            LB.EDGE_ONLY, SimpleGPUSchedule.edge_blocking_type.BLOCKED, 0x42000)), False
+    if app == "cc":  # cc.cpp:86-88
+        return s().configDirection(D.PUSH).configLoadBalancing(LB.EDGE_ONLY), False
+    if app == "bc":  # bc.cpp:131-156
+        if power:
+            s1 = s().configDirection(D.PUSH).configLoadBalancing(LB.TWCE)
+            s2 = (s().configDirection(D.PULL, PR_.BITMAP).configLoadBalancing(LB.TWCE)
+                  .configFrontierCreation(FC.BITMAP))
+            return HybridGPUSchedule(s1, s2).bindThreshold(threshold), False
+        return s().configDirection(D.PUSH).configLoadBalancing(LB.TWCE), True
+    raise ValueError(f"unknown app {app!r}")
+
+
+# ------------------------------------------------------------------ graphs
+K_RAND_SEED = 27491095  # GAPBS kRandSeed (infra_gapbs/util.h:22)
+
+
+def _np_ptr(a: Optional[np.ndarray]):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class HostGraph:
+    """Host CSR built like GAPBS's builder (sorted, deduplicated, no self-loops)."""
+
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+
+    @classmethod
+    def _make(cls, fn: str, *args) -> "HostGraph":
+        h = C.c_void_p()
+        call(fn, *args, C.byref(h))
+        return cls(h)
+
+    @classmethod
+    def rmat(cls, scale: int, degree: int = 16, a: float = 0.57, b: float = 0.19,
+             c: float = 0.19, seed: int = K_RAND_SEED, symmetrize: bool = False,
+             wmin: int = 1, wmax: int = 255) -> "HostGraph":
+        return cls._make("gg_host_graph_rmat", scale, degree, a, b, c, seed, int(symmetrize),
+                         wmin, wmax)
+
+    @classmethod
+    def grid(cls, rows: int, cols: int, seed: int = K_RAND_SEED, wmin: int = 1,
+             wmax: int = 1000) -> "HostGraph":
+        return cls._make("gg_host_graph_grid", rows, cols, seed, wmin, wmax)
+
+    @classmethod
+    def from_edges(cls, num_vertices: int, u, v, w=None, symmetrize: bool = False) -> "HostGraph":
+        u = np.ascontiguousarray(u, dtype=np.int32)
+        v = np.ascontiguousarray(v, dtype=np.int32)
+        w = None if w is None else np.ascontiguousarray(w, dtype=np.int32)
+        return cls._make("gg_host_graph_from_edges", num_vertices, len(u), _np_ptr(u), _np_ptr(v),
+                         _np_ptr(w), int(symmetrize))
+
+    @classmethod
+    def from_csr(cls, offsets, dst, weights=None) -> "HostGraph":
+        off = np.ascontiguousarray(offsets, dtype=np.int32)
+        dst = np.ascontiguousarray(dst, dtype=np.int32)
+        w = None if weights is None else np.ascontiguousarray(weights, dtype=np.int32)
+        return cls._make("gg_host_graph_from_csr", len(off) - 1, len(dst), _np_ptr(off),
+                         _np_ptr(dst), _np_ptr(w))
+
+    @classmethod
+    def load(cls, path: str, symmetrize: bool = False) -> "HostGraph":
+        return cls._make("gg_host_graph_load", str(path).encode(), int(symmetrize))
+
+    def save_bin(self, path: str) -> None:
+        call("gg_host_graph_save_bin", self._h, str(path).encode())
+
+    @property
+    def num_vertices(self) -> int:
+        v, e = C.c_int32(), C.c_int64()
+        call("gg_host_graph_info", self._h, C.byref(v), C.byref(e))
+        return v.value
+
+    @property
+    def num_edges(self) -> int:
+        v, e = C.c_int32(), C.c_int64()
+        call("gg_host_graph_info", self._h, C.byref(v), C.byref(e))
+        return e.value
+
+    def _view(self, fn: str, n: int) -> np.ndarray:
+        p = getattr(lib(), fn)(self._h)
+        if n == 0:
+            return np.zeros(0, dtype=np.int32)
+        return np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_int32)), shape=(n,))
+
+    @property
+    def offsets(self) -> np.ndarray:
+        """Zero-copy view (valid while this object lives)."""
+        return self._view("gg_host_graph_offsets", self.num_vertices + 1)
+
+    @property
+    def dst(self) -> np.ndarray:
+        return self._view("gg_host_graph_dst", self.num_edges)
+
+    @property
+    def weights(self) -> np.ndarray:
+        return self._view("gg_host_graph_weights", self.num_edges)
+
+    def out_degrees(self) -> np.ndarray:
+        return np.diff(self.offsets)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and lib is not None:
+            try:
+                lib().gg_host_graph_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
+class GraphT:
+    """A graph resident in HBM (graphit_runtime::GraphT<int>)."""
+
+    def __init__(self, host: HostGraph | None = None, *, offsets=None, dst=None, weights=None,
+                 symmetric: bool = False):
+        if host is not None:
+            offsets, dst, weights = host.offsets, host.dst, host.weights
+        self._keep = (offsets, dst, weights)
+        V = (offsets.numel() if hasattr(offsets, "numel") else len(offsets)) - 1
+        E = dst.numel() if hasattr(dst, "numel") else len(dst)
+        h = C.c_void_p()
+        call("gg_graph_create", _ptr(offsets), _ptr(dst), _ptr(weights), V, E,
+             1 if symmetric else 0, C.byref(h))
+        self._h = h
+        self._keep = None
+        self.num_vertices, self.num_edges, self.symmetric = V, E, symmetric
+
+    @property
+    def handle(self):
+        return self._h
+
+    def get_transposed_graph(self) -> "GraphT":
+        call("gg_graph_transpose", self._h)
+        return self
+
+    def get_blocked_graph(self, block_size: int) -> "GraphT":
+        call("gg_graph_blocked", self._h, block_size)
+        return self
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        call("gg_graph_set_stream", self._h, C.c_void_p(stream_ptr) if stream_ptr else None)
+
+    def sync(self) -> None:
+        call("gg_graph_sync", self._h)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().gg_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _ptr(a):
+    """Raw pointer of a numpy array or torch tensor (None passes NULL)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    return C.c_void_p(np.ascontiguousarray(a).ctypes.data)
+
+
+# ----------------------------------------------------------- vertex subsets
+class VertexSubset:
+    """graphit_runtime::VertexFrontier."""
+
+    SPARSE, BITMAP, BOOLMAP = 0, 1, 2
+
+    def __init__(self, g: GraphT, init_all: bool = False):
+        self.g = g
+        h = C.c_void_p()
+        call("gg_frontier_create", g.handle, int(init_all), C.byref(h))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def addVertex(self, v: int) -> None:
+        call("gg_frontier_add", self._h, v)
+
+    def size(self) -> int:
+        n = C.c_int32()
+        call("gg_frontier_size", self._h, C.byref(n))
+        return n.value
+
+    def format(self) -> int:
+        n = C.c_int32()
+        call("gg_frontier_format", self._h, C.byref(n))
+        return n.value
+
+    def to_sparse(self):
+        call("gg_frontier_to_sparse", self._h)
+
+    def to_bitmap(self):
+        call("gg_frontier_to_bitmap", self._h)
+
+    def to_boolmap(self):
+        call("gg_frontier_to_boolmap", self._h)
+
+    def dedup(self):
+        call("gg_frontier_dedup", self._h)
+
+    def clear(self):
+        call("gg_frontier_clear", self._h)
+
+    def read(self) -> np.ndarray:
+        n = C.c_int32()
+        call("gg_frontier_read", self._h, None, 0, C.byref(n))
+        out = np.empty(n.value, dtype=np.int32)
+        call("gg_frontier_read", self._h, _ptr(out), n.value, C.byref(n))
+        return out
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                lib().gg_frontier_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- the apps
+def _stats(st: L.gg_stats) -> dict:
+    return st.as_dict()
+
+
+def _resolve(app: str, schedule, fuse):
+    if schedule is None:
+        schedule, dflt_fuse = default_schedule(app)
+        fuse = dflt_fuse if fuse is None else fuse
+    return app_schedule(schedule, bool(fuse))
+
+
+def bfs(g: GraphT, src: int, schedule=None, fuse=None, with_parent: bool = False):
+    """apps/bfs.cpp: returns (depth, parent|None, stats)."""
+    V = g.num_vertices
+    depth = np.empty(V, dtype=np.int32)
+    parent = np.empty(V, dtype=np.int32) if with_parent else None
+    st = L.gg_stats()
+    a = _resolve("bfs", schedule, fuse)
+    call("gg_bfs", g.handle, C.byref(a), src, _ptr(depth), _ptr(parent), C.byref(st))
+    return depth, parent, _stats(st)
+
+
+def sssp(g: GraphT, src: int, delta: int, schedule=None, fuse=None):
+    """apps/sssp.cpp: returns (dist, stats); INT_MAX marks unreached."""
+    dist = np.empty(g.num_vertices, dtype=np.int32)
+    st = L.gg_stats()
+    a = _resolve("sssp", schedule, fuse)
+    call("gg_sssp", g.handle, C.byref(a), src, delta, _ptr(dist), C.byref(st))
+    return dist, _stats(st)
+
+
+def pagerank(g: GraphT, iters: int = 20, damping: float = 0.85, schedule=None):
+    """apps/pr.cpp: returns (rank, stats)."""
+    rank = np.empty(g.num_vertices, dtype=np.float32)
+    st = L.gg_stats()
+    a = _resolve("pr", schedule, False)
+    call("gg_pagerank", g.handle, C.byref(a), iters, damping, _ptr(rank), C.byref(st))
+    return rank, _stats(st)
+
+
+def cc(g: GraphT, schedule=None):
+    """apps/cc.cpp: returns (labels, stats); label = min vertex id of the component."""
+    labels = np.empty(g.num_vertices, dtype=np.int32)
+    st = L.gg_stats()
+    a = _resolve("cc", schedule, False)
+    call("gg_cc", g.handle, C.byref(a), _ptr(labels), C.byref(st))
+    return labels, _stats(st)
+
+
+def bc(g: GraphT, src: int, schedule=None, fuse=None):
+    """apps/bc.cpp: returns (dependences fp32, stats)."""
+    dep = np.empty(g.num_vertices, dtype=np.float32)
+    st = L.gg_stats()
+    a = _resolve("bc", schedule, fuse)
+    call("gg_bc", g.handle, C.byref(a), src, _ptr(dep), C.byref(st))
+    return dep, _stats(st)

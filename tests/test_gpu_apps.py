@@ -1,0 +1,280 @@
+"""GPU parity of the five apps against the oracle, through the C ABI.
+
+Bit-exact: BFS depths (and a valid parent tree), SSSP int32 distances, CC
+labels.  PageRank and BC: relative L1 <= 1e-6 against the FP64 oracle.
+Every load-balancing strategy, both directions, every frontier representation
+and the fused/unfused loops must give the same results.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from easy_graphit_gb300 import (GraphT, HostGraph, HybridGPUSchedule, SimpleGPUSchedule, bc, bfs,
+                                cc, default_schedule, pagerank, sssp)
+from tests.conftest import rel_l1
+
+pytestmark = pytest.mark.gpu
+
+T = SimpleGPUSchedule
+LBS = [T.load_balancing_type.VERTEX_BASED, T.load_balancing_type.TWC, T.load_balancing_type.TWCE,
+       T.load_balancing_type.WM, T.load_balancing_type.CM, T.load_balancing_type.STRICT,
+       T.load_balancing_type.EDGE_ONLY, T.load_balancing_type.ETWC]
+PR_TOL = 1e-6
+BC_TOL = 1e-6
+
+
+def sched(direction=T.direction_type.PUSH, lb=T.load_balancing_type.TWCE,
+          creation=T.frontier_creation_type.SPARSE, pull_rep=T.pull_frontier_rep_type.BITMAP,
+          blocked=0, cta=512):
+    s = SimpleGPUSchedule()
+    s.configDirection(direction, pull_rep)
+    if lb == T.load_balancing_type.EDGE_ONLY and blocked:
+        s.configLoadBalancing(lb, T.edge_blocking_type.BLOCKED, blocked)
+    else:
+        s.configLoadBalancing(lb)
+    s.configFrontierCreation(creation)
+    s.cta_size = cta
+    return s
+
+
+_CACHE = {}
+
+
+def graph(kind):
+    if kind not in _CACHE:
+        if kind == "sym12":
+            hg = HostGraph.rmat(12, 16, symmetrize=True)
+        elif kind == "dir12":
+            hg = HostGraph.rmat(12, 16)
+        elif kind == "sym16":
+            hg = HostGraph.rmat(16, 16, symmetrize=True)
+        elif kind == "dir16":
+            hg = HostGraph.rmat(16, 16)
+        elif kind == "grid":
+            hg = HostGraph.grid(64, 48)
+        else:
+            raise KeyError(kind)
+        sym = kind.startswith("sym") or kind == "grid"
+        _CACHE[kind] = (hg, GraphT(hg, symmetric=sym),
+                        (np.array(hg.offsets), np.array(hg.dst), np.array(hg.weights)))
+    return _CACHE[kind]
+
+
+def hub(off):
+    return int(np.argmax(np.diff(off)))
+
+
+# ------------------------------------------------------------------ BFS
+@pytest.mark.parametrize("lb", LBS, ids=lambda x: x.name)
+@pytest.mark.parametrize("kind", ["sym12", "dir12"])
+def test_bfs_push_every_lb(kind, lb):
+    hg, g, (off, dst, _) = graph(kind)
+    s = hub(off)
+    ref = oracle.bfs(off, dst, s)
+    depth, parent, st = bfs(g, s, sched(lb=lb), fuse=False, with_parent=True)
+    np.testing.assert_array_equal(depth, ref)
+    assert oracle.bfs_check_parent(off, dst, s, depth, parent) == 0
+    assert st["iterations"] == ref.max() + 1
+
+
+@pytest.mark.parametrize("lb", [T.load_balancing_type.VERTEX_BASED, T.load_balancing_type.TWCE,
+                                T.load_balancing_type.WM, T.load_balancing_type.CM],
+                         ids=lambda x: x.name)
+@pytest.mark.parametrize("kind", ["sym16", "dir16", "grid"])
+def test_bfs_fused(kind, lb):
+    hg, g, (off, dst, _) = graph(kind)
+    s = hub(off)
+    ref = oracle.bfs(off, dst, s)
+    depth, parent, st = bfs(g, s, sched(lb=lb), fuse=True, with_parent=True)
+    np.testing.assert_array_equal(depth, ref)
+    assert oracle.bfs_check_parent(off, dst, s, depth, parent) == 0
+    assert st["edges_traversed"] == oracle.reached_edges(off, ref)
+
+
+@pytest.mark.parametrize("creation", list(T.frontier_creation_type), ids=lambda x: x.name)
+@pytest.mark.parametrize("pull_rep", list(T.pull_frontier_rep_type), ids=lambda x: x.name)
+@pytest.mark.parametrize("lb", [T.load_balancing_type.VERTEX_BASED, T.load_balancing_type.WM,
+                                T.load_balancing_type.TWCE, T.load_balancing_type.EDGE_ONLY],
+                         ids=lambda x: x.name)
+def test_bfs_pull_every_representation(creation, pull_rep, lb):
+    hg, g, (off, dst, _) = graph("dir12")
+    s = hub(off)
+    ref = oracle.bfs(off, dst, s)
+    sc = sched(direction=T.direction_type.PULL, lb=lb, creation=creation, pull_rep=pull_rep)
+    depth, parent, _ = bfs(g, s, sc, fuse=False, with_parent=True)
+    np.testing.assert_array_equal(depth, ref)
+    assert oracle.bfs_check_parent(off, dst, s, depth, parent) == 0
+
+
+@pytest.mark.parametrize("threshold", [0.0, 0.01, 0.12, 1.0])
+def test_bfs_hybrid_power_schedule(threshold):
+    hg, g, (off, dst, _) = graph("sym16")
+    s = hub(off)
+    ref = oracle.bfs(off, dst, s)
+    hs, _ = default_schedule("bfs", power=True, threshold=threshold)
+    depth, parent, st = bfs(g, s, hs, fuse=False, with_parent=True)
+    np.testing.assert_array_equal(depth, ref)
+    assert oracle.bfs_check_parent(off, dst, s, depth, parent) == 0
+    if threshold == 0.0:
+        assert st["push_iterations"] <= 1
+    if threshold == 1.0:
+        assert st["pull_iterations"] == 0
+
+
+def test_bfs_golden_reference_depths(golden):
+    hg = HostGraph.rmat(12, 16)
+    g = GraphT(hg)
+    for i, s in enumerate(golden["sources/rmat12_k16_dir"]):
+        depth, _, _ = bfs(g, int(s))
+        np.testing.assert_array_equal(depth, golden["bfs/rmat12_k16_dir"][i])
+
+
+# ------------------------------------------------------------------ SSSP
+@pytest.mark.parametrize("delta", [1, 8, 32, 128])
+def test_sssp_golden_reference_distances(golden, delta):
+    for name, (scale, sym) in {"rmat10_k16_sym": (10, True), "rmat12_k16_dir": (12, False)}.items():
+        hg = HostGraph.rmat(scale, 16, symmetrize=sym)
+        g = GraphT(hg, symmetric=sym)
+        for fuse in (True, False):
+            for i, s in enumerate(golden[f"sources/{name}"]):
+                d, _ = sssp(g, int(s), delta, fuse=fuse)
+                np.testing.assert_array_equal(d, golden[f"sssp/{name}/d{delta}"][i])
+
+
+@pytest.mark.parametrize("lb", LBS, ids=lambda x: x.name)
+@pytest.mark.parametrize("creation", list(T.frontier_creation_type), ids=lambda x: x.name)
+def test_sssp_every_lb_and_creation(lb, creation):
+    hg, g, (off, dst, w) = graph("dir12")
+    s = hub(off)
+    ref = oracle.sssp_dijkstra(off, dst, w, s)
+    d, st = sssp(g, s, 32, sched(lb=lb, creation=creation), fuse=False)
+    np.testing.assert_array_equal(d, ref)
+
+
+@pytest.mark.parametrize("lb", [T.load_balancing_type.VERTEX_BASED, T.load_balancing_type.TWCE,
+                                T.load_balancing_type.WM, T.load_balancing_type.CM],
+                         ids=lambda x: x.name)
+@pytest.mark.parametrize("delta", [1, 128])
+def test_sssp_fused_larger(lb, delta):
+    hg, g, (off, dst, w) = graph("dir16")
+    s = hub(off)
+    ref = oracle.sssp_dijkstra(off, dst, w, s)
+    d, st = sssp(g, s, delta, sched(lb=lb), fuse=True)
+    np.testing.assert_array_equal(d, ref)
+    _, adv = oracle.sssp_delta_gpu(off, dst, w, s, delta)
+    assert st["bucket_advances"] == adv
+
+
+def test_sssp_grid_and_power_schedule():
+    hg, g, (off, dst, w) = graph("grid")
+    for s in [0, 1000, 3071]:
+        ref = oracle.sssp_dijkstra(off, dst, w, s)
+        for delta in [8, 128]:
+            d, _ = sssp(g, s, delta)  # default: PUSH SPARSE VERTEX_BASED fused
+            np.testing.assert_array_equal(d, ref)
+            ps, fuse = default_schedule("sssp", power=True)
+            d, _ = sssp(g, s, delta, ps, fuse=fuse)
+            np.testing.assert_array_equal(d, ref)
+
+
+# --------------------------------------------------------------- PageRank
+@pytest.mark.parametrize("sc", [
+    "default",
+    sched(direction=T.direction_type.PULL, lb=T.load_balancing_type.EDGE_ONLY),
+    sched(direction=T.direction_type.PUSH, lb=T.load_balancing_type.EDGE_ONLY, blocked=1000),
+    sched(direction=T.direction_type.PULL, lb=T.load_balancing_type.WM),
+    sched(direction=T.direction_type.PULL, lb=T.load_balancing_type.VERTEX_BASED),
+    sched(direction=T.direction_type.PUSH, lb=T.load_balancing_type.TWCE),
+    sched(direction=T.direction_type.PULL, lb=T.load_balancing_type.CM),
+], ids=["default", "pull_edge_only", "push_edge_only_blocked", "pull_wm", "pull_vertex",
+        "push_twce", "pull_cm"])
+def test_pagerank(sc):
+    hg, g, (off, dst, _) = graph("dir16")
+    ref = oracle.pagerank(off, dst, 20, float(np.float32(0.85)))
+    r, st = pagerank(g, 20, 0.85, None if sc == "default" else sc)
+    assert rel_l1(r, ref) <= PR_TOL, rel_l1(r, ref)
+
+
+# --------------------------------------------------------------------- CC
+@pytest.mark.parametrize("lb", LBS, ids=lambda x: x.name)
+@pytest.mark.parametrize("kind", ["sym12", "dir12"])
+def test_cc(kind, lb):
+    hg, g, (off, dst, _) = graph(kind)
+    ref = oracle.cc(off, dst)
+    labels, _ = cc(g, sched(lb=lb))
+    np.testing.assert_array_equal(labels, ref)
+
+
+def test_cc_default_large():
+    hg, g, (off, dst, _) = graph("sym16")
+    labels, st = cc(g)
+    np.testing.assert_array_equal(labels, oracle.cc(off, dst))
+
+
+# --------------------------------------------------------------------- BC
+@pytest.mark.parametrize("power", [False, True])
+@pytest.mark.parametrize("kind", ["sym12", "sym16", "grid"])
+def test_bc(kind, power):
+    hg, g, (off, dst, _) = graph(kind)
+    s = hub(off)
+    ref = oracle.bc(off, dst, s)
+    sch, fuse = default_schedule("bc", power=power, threshold=0.05)
+    dep, st = bc(g, s, sch, fuse=fuse)
+    assert rel_l1(dep, ref) <= BC_TOL, rel_l1(dep, ref)
+
+
+@pytest.mark.parametrize("lb", LBS, ids=lambda x: x.name)
+def test_bc_every_lb(lb):
+    hg, g, (off, dst, _) = graph("sym12")
+    s = hub(off)
+    ref = oracle.bc(off, dst, s)
+    dep, _ = bc(g, s, sched(lb=lb), fuse=False)
+    assert rel_l1(dep, ref) <= BC_TOL, rel_l1(dep, ref)
+
+
+# ------------------------------------------------------------- edge cases
+def test_edge_cases():
+    # isolated source, empty edge set, self-loops and duplicates kept by from_csr
+    hg = HostGraph.from_csr([0, 0, 0, 0], [], None)
+    g = GraphT(hg)
+    depth, _, _ = bfs(g, 1)
+    np.testing.assert_array_equal(depth, [-1, 0, -1])
+    d, _ = sssp(g, 2, 4)
+    np.testing.assert_array_equal(d, [2**31 - 1, 2**31 - 1, 0])
+    labels, _ = cc(g)
+    np.testing.assert_array_equal(labels, [0, 1, 2])
+    off = [0, 3, 4, 4]
+    dst = [0, 1, 1, 2]  # self-loop 0->0, duplicate 0->1
+    hg = HostGraph.from_csr(off, dst, [1, 5, 2, 1])
+    g = GraphT(hg)
+    depth, parent, _ = bfs(g, 0, with_parent=True)
+    np.testing.assert_array_equal(depth, [0, 1, 2])
+    d, _ = sssp(g, 0, 1)
+    np.testing.assert_array_equal(d, [0, 2, 3])
+    # path graph: deep
+    n = 3000
+    hg = HostGraph.from_edges(n, np.arange(n - 1), np.arange(1, n), symmetrize=True)
+    g = GraphT(hg, symmetric=True)
+    depth, _, st = bfs(g, 0)
+    np.testing.assert_array_equal(depth, np.arange(n))
+    dep, _ = bc(g, 0)
+    ref = oracle.bc(np.array(hg.offsets), np.array(hg.dst), 0)
+    assert rel_l1(dep, ref) <= BC_TOL
+    # star: one hub with a huge degree
+    n = 200000
+    hg = HostGraph.from_edges(n, np.zeros(n - 1, dtype=np.int32), np.arange(1, n), symmetrize=True)
+    g = GraphT(hg, symmetric=True)
+    for lb in LBS:
+        depth, _, _ = bfs(g, 5, sched(lb=lb), fuse=False)
+        assert depth[0] == 1 and depth[5] == 0 and (depth[1:] == 2).sum() == n - 2
+
+
+def test_deterministic_outputs():
+    hg, g, (off, dst, w) = graph("dir16")
+    s = hub(off)
+    r1, _ = pagerank(g, 20, 0.85, sched(direction=T.direction_type.PULL, lb=T.load_balancing_type.WM))
+    r2, _ = pagerank(g, 20, 0.85, sched(direction=T.direction_type.PULL, lb=T.load_balancing_type.WM))
+    d1, _ = sssp(g, s, 8)
+    d2, _ = sssp(g, s, 8)
+    np.testing.assert_array_equal(d1, d2)
+    assert rel_l1(r1, r2) < 1e-6

@@ -1,0 +1,132 @@
+"""The oracle against the reference's golden data and hand-computed answers (CPU)."""
+import numpy as np
+import pytest
+
+import oracle
+from tests.conftest import INT_MAX, rel_l1
+
+DELTAS = [1, 8, 32, 128]
+
+
+def _g(golden, name):
+    from easy_graphit_gb300 import HostGraph
+    scale, deg, sym = {"rmat10_k16_sym": (10, 16, True), "rmat12_k16_dir": (12, 16, False)}[name]
+    hg = HostGraph.rmat(scale, deg, symmetrize=sym)
+    return np.array(hg.offsets), np.array(hg.dst), np.array(hg.weights)
+
+
+@pytest.mark.parametrize("name", ["rmat10_k16_sym", "rmat12_k16_dir"])
+@pytest.mark.parametrize("delta", DELTAS)
+def test_sssp_oracles_match_reference(golden, name, delta):
+    off, dst, w = _g(golden, name)
+    ref = golden[f"sssp/{name}/d{delta}"]
+    for i, s in enumerate(golden[f"sources/{name}"]):
+        np.testing.assert_array_equal(oracle.sssp_dijkstra(off, dst, w, int(s)), ref[i])
+        d, adv = oracle.sssp_delta_gpu(off, dst, w, int(s), delta)
+        np.testing.assert_array_equal(d, ref[i])
+        assert adv >= 1
+        np.testing.assert_array_equal(oracle.sssp_ordered(off, dst, w, int(s), delta, 4), ref[i])
+
+
+@pytest.mark.parametrize("name", ["rmat10_k16_sym", "rmat12_k16_dir"])
+def test_bfs_oracle_matches_reference_unit_weight_sssp(golden, name):
+    off, dst, _ = _g(golden, name)
+    ref = golden[f"bfs/{name}"]
+    for i, s in enumerate(golden[f"sources/{name}"]):
+        np.testing.assert_array_equal(oracle.bfs(off, dst, int(s)), ref[i])
+        np.testing.assert_array_equal(oracle.bfs_omp(off, dst, int(s), 4), ref[i])
+
+
+def test_bfs_parent_checker_catches_bad_parent(golden):
+    off, dst, _ = _g(golden, "rmat10_k16_sym")
+    s = int(golden["sources/rmat10_k16_sym"][0])
+    depth = oracle.bfs(off, dst, s)
+    # Build a valid parent array on the CPU, then plant one mistake.
+    parent = np.full(len(depth), -1, dtype=np.int32)
+    parent[s] = s
+    for u in range(len(depth)):
+        for k in range(off[u], off[u + 1]):
+            v = dst[k]
+            if depth[v] == depth[u] + 1 and parent[v] == -1:
+                parent[v] = u
+    assert oracle.bfs_check_parent(off, dst, s, depth, parent) == 0
+    v = int(np.where(depth == 2)[0][0])
+    parent[v] = s
+    assert oracle.bfs_check_parent(off, dst, s, depth, parent) == 1
+
+
+def _csr(V, edges, sym=False):
+    from easy_graphit_gb300 import HostGraph
+    u = [a for a, b in edges]
+    v = [b for a, b in edges]
+    hg = HostGraph.from_edges(V, u, v, symmetrize=sym)
+    return np.array(hg.offsets), np.array(hg.dst)
+
+
+def test_pagerank_known_answers():
+    off, dst = _csr(3, [(0, 1), (1, 2), (2, 0)])
+    np.testing.assert_allclose(oracle.pagerank(off, dst, 20), [1 / 3] * 3, rtol=1e-12)
+    off, dst = _csr(2, [(0, 1)])  # vertex 1 is a sink: no dangling redistribution
+    r1 = oracle.pagerank(off, dst, 1)
+    np.testing.assert_allclose(r1, [0.075, 0.075 + 0.85 * 0.5], rtol=1e-12)
+    r2 = oracle.pagerank(off, dst, 2)
+    np.testing.assert_allclose(r2, [0.075, 0.075 + 0.85 * 0.075], rtol=1e-12)
+
+
+def test_cc_known_answers():
+    off, dst = _csr(6, [(2, 1), (1, 0), (4, 3)])
+    np.testing.assert_array_equal(oracle.cc(off, dst), [0, 0, 0, 3, 3, 5])
+    lab, rounds = oracle.cc_labelprop(off, dst)
+    np.testing.assert_array_equal(lab, [0, 0, 0, 3, 3, 5])
+    assert rounds >= 1
+
+
+@pytest.mark.parametrize("name", ["rmat10_k16_sym", "rmat12_k16_dir"])
+def test_cc_labelprop_restatement_equals_union_find(golden, name):
+    off, dst, _ = _g(golden, name)
+    lab, _ = oracle.cc_labelprop(off, dst)
+    np.testing.assert_array_equal(lab, oracle.cc(off, dst))
+    np.testing.assert_array_equal(oracle.cc_omp(off, dst, 4), oracle.cc(off, dst))
+
+
+def test_bc_known_answers():
+    off, dst = _csr(3, [(0, 1), (1, 2)], sym=True)  # path 0-1-2
+    np.testing.assert_allclose(oracle.bc(off, dst, 0), [2, 1, 0])
+    off, dst = _csr(4, [(0, 1), (0, 2), (0, 3)], sym=True)  # star, source = leaf 1
+    np.testing.assert_allclose(oracle.bc(off, dst, 1), [2, 3, 0, 0])
+    off, dst = _csr(4, [(0, 1), (0, 2), (1, 3), (2, 3)], sym=True)  # diamond
+    np.testing.assert_allclose(oracle.bc(off, dst, 0), [3, 0.5, 0.5, 0])
+    off, dst = _csr(3, [(1, 2)], sym=True)  # isolated source
+    np.testing.assert_allclose(oracle.bc(off, dst, 0), [0, 0, 0])
+
+
+def test_bc_matches_brandes_dependencies(golden):
+    nx = pytest.importorskip("networkx")
+    from networkx.algorithms.centrality import betweenness as B
+    off, dst, _ = _g(golden, "rmat10_k16_sym")
+    G = nx.DiGraph()
+    G.add_nodes_from(range(len(off) - 1))
+    for u in range(len(off) - 1):
+        for k in range(off[u], off[u + 1]):
+            G.add_edge(u, int(dst[k]))
+    for s in golden["sources/rmat10_k16_sym"][:2]:
+        s = int(s)
+        S, P, sigma, _ = B._single_source_shortest_path_basic(G, s)
+        acc = dict.fromkeys(G, 0.0)
+        acc, _ = B._accumulate_basic(acc, S, P, sigma, s)
+        ref = np.array([acc[v] for v in range(len(off) - 1)])
+        got = oracle.bc(off, dst, s)
+        mask = np.arange(len(ref)) != s
+        assert rel_l1(got[mask], ref[mask]) < 1e-12
+
+
+def test_sssp_matches_scipy(golden):
+    sp = pytest.importorskip("scipy.sparse")
+    csg = pytest.importorskip("scipy.sparse.csgraph")
+    off, dst, w = _g(golden, "rmat12_k16_dir")
+    V = len(off) - 1
+    A = sp.csr_matrix((w.astype(np.float64), dst, off), shape=(V, V))
+    s = int(golden["sources/rmat12_k16_dir"][0])
+    d = csg.dijkstra(A, indices=s)
+    ref = np.where(np.isinf(d), INT_MAX, d).astype(np.int64)
+    np.testing.assert_array_equal(oracle.sssp_dijkstra(off, dst, w, s), ref)
