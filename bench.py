@@ -1,0 +1,357 @@
+#!/usr/bin/env python3
+"""Throughput of the GraphIt edge-traversal path on GB300, in GTEPS.
+
+Workload (default, one GPU): SSSP delta-stepping on a directed R-MAT graph of
+scale 22, edge factor 16 (a/b/c = 0.57/0.19/0.19, GAPBS seed 27491095), int32
+weights U[1,255]; 32 sources from GAPBS's SourcePicker; one step = SSSP from all
+32 sources.  Inputs are synthetic (the reference's datasets are not available).
+TEPS counts each reached vertex's out-edges once per source (E_r).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+  torchrun ... bench.py --gpus N     (one rank per GPU; sources shard by rank)
+
+The default arm runs the engine (libgg.so) through its C ABI; `--impl
+reference` times the reference's CPU delta-stepping (GAPBS
+OrderedProcessingOperatorNoMerge, as ported in oracle/) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+INT_MAX = 2**31 - 1
+SCALE, DEGREE = 22, 16
+N_SOURCES = 32
+DELTAS = (1, 8, 32, 128)
+METRIC = "GTEPS per app at 1 GB300: learned+batched vs plain schedule, exact results"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--scale", type=int, default=SCALE)
+    p.add_argument("--delta", type=int, default=0, help="0 = pick by a short autotune")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_graph(scale):
+    from easy_graphit_gb300 import HostGraph
+    return HostGraph.rmat(scale, DEGREE)
+
+
+def reached_stats(off, dist):
+    reached = (dist != INT_MAX)
+    deg = np.diff(off)
+    return int(reached.sum()), int(deg[reached].sum())
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# -------------------------------------------------------------- CPU legs
+def cpu_sssp(off, dst, w, sources, delta, budget_s):
+    """GAPBS ordered-processing SSSP (oracle port) on the host cores over a
+    bounded sample of the sources; returns (GTEPS, threads, n_sources, seconds)."""
+    import oracle
+    threads = os.cpu_count() or 1
+    edges = 0
+    t0 = time.perf_counter()
+    n = 0
+    for s in sources:
+        d = oracle.sssp_ordered(off, dst, w, int(s), delta, threads)
+        edges += reached_stats(off, d)[1]
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return edges / dt / 1e9, threads, n, dt
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "sssp_fused_vertex_rmat22.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+# ------------------------------------------------------------------- arms
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if world > 1 and rank != 0:
+        return
+    hg = make_graph(args.scale)
+    off, dst, w = np.array(hg.offsets), np.array(hg.dst), np.array(hg.weights)
+    sources = hg.pick_sources(N_SOURCES)
+    delta = args.delta or 32
+    per_step = 2  # bounded sample of the 32 sources per step
+    vals = []
+    for i in range(args.warmup + args.steps):
+        srcs = [sources[(2 * i + k) % N_SOURCES] for k in range(per_step)]
+        g, threads, n, dt = cpu_sssp(off, dst, w, srcs, delta, 1e9)
+        if i >= args.warmup:
+            vals.append(g)
+    value = float(np.mean(vals))
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GTEPS",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic",
+        "config": {"workload": f"sssp_delta_stepping_rmat{args.scale}_k16_directed",
+                   "sources": N_SOURCES, "delta": delta, "weights": "U[1,255]"},
+        "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": threads, "kind": "port",
+                         "sample": f"{per_step} of the {N_SOURCES} sources per step "
+                                   f"(GAPBS OrderedProcessingOperatorNoMerge port, all host threads)"},
+        "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def run_gb300(args):
+    import torch
+    import torch.distributed as dist
+
+    from easy_graphit_gb300 import GraphT, _lib as L, app_schedule, default_schedule
+    from easy_graphit_gb300.graphit import _ptr
+    import ctypes as C
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    hg = make_graph(args.scale)
+    off, dst, w = np.array(hg.offsets), np.array(hg.dst), np.array(hg.weights)
+    V, E = hg.num_vertices, hg.num_edges
+    # weak scaling: every rank traverses its own 32 sources on its own replica
+    sources = hg.pick_sources(N_SOURCES, seed=27491095 + rank)
+
+    g = GraphT(hg)
+    stream = torch.cuda.current_stream(dev)
+    g.set_stream(stream.cuda_stream)
+    sch, fuse = default_schedule("sssp")  # PUSH, SPARSE, VERTEX_BASED, fused (sssp.cpp:76-79)
+    a = app_schedule(sch, fuse)
+    dist_dev = torch.empty((N_SOURCES, V), dtype=torch.int32, device=dev)
+    st = L.gg_stats()
+
+    def one(src, out_ptr, stats=True):
+        L.call("gg_sssp", g.handle, C.byref(a), int(src), delta, out_ptr,
+               C.byref(st) if stats else None)
+        return st.loop_ms
+
+    # Delta: all four give identical distances; pick the fastest on one source.
+    delta = args.delta
+    if not delta:
+        best = None
+        for d in DELTAS:
+            delta = d
+            one(sources[0], C.c_void_p(dist_dev[0].data_ptr()))
+            t = one(sources[0], C.c_void_p(dist_dev[0].data_ptr()))
+            if best is None or t < best[0]:
+                best = (t, d)
+        delta = best[1]
+
+    # Algorithmic work per source (untimed pass): E_r, V_r.
+    er, vr, loop_ms = [], [], []
+    for i, s in enumerate(sources):
+        one(s, C.c_void_p(dist_dev[i].data_ptr()))
+        d = dist_dev[i].cpu().numpy()
+        v_r, e_r = reached_stats(off, d)
+        er.append(e_r)
+        vr.append(v_r)
+    total_edges = float(sum(er))
+
+    def step(out_base, stride_bytes):
+        for i, s in enumerate(sources):
+            one(s, C.c_void_p(out_base + i * stride_bytes))
+
+    base = dist_dev.data_ptr()
+    for _ in range(args.warmup):
+        step(base, V * 4)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    l0 = L.lib().gg_kernel_launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            for i, s in enumerate(sources):
+                one(s, C.c_void_p(base + i * V * 4))
+                loop_ms.append(st.loop_ms)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = int(L.lib().gg_kernel_launches() - l0)
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = total_edges * world / (ms_per_step / 1e3) / 1e9
+
+    # End to end through the C ABI with host buffers: upload the CSR from
+    # pinned host memory, run the 32 sources with distances written to pinned
+    # host memory, release the graph -- all inside the timed region.
+    pin = lambda a_: torch.from_numpy(a_).pin_memory()
+    h_off, h_dst, h_w = pin(off), pin(dst), pin(w)
+    h_out = torch.empty((N_SOURCES, V), dtype=torch.int32).pin_memory()
+    h2d = (off.nbytes + dst.nbytes + w.nbytes)
+    d2h = N_SOURCES * V * 4
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ge = GraphT(offsets=h_off, dst=h_dst, weights=h_w)
+        ge.set_stream(stream.cuda_stream)
+        for i, s in enumerate(sources):
+            L.call("gg_sssp", ge.handle, C.byref(a), int(s), delta,
+                   C.c_void_p(h_out.data_ptr() + i * V * 4), None)
+        ge.close()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    assert np.array_equal(h_out[0].numpy(), dist_dev[0].cpu().numpy())
+    e2e_val = total_edges * world / (e2e_ms / 1e3) / 1e9
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    peak, peak_kind = peaks()
+    alg_bytes = [12.0 * e + 16.0 * v for e, v in zip(er, vr)]
+    lm = np.array(loop_ms).reshape(args.steps, N_SOURCES).mean(axis=0)  # per source
+    achieved = float(np.sum(alg_bytes) / (np.sum(lm) / 1e3) / 1e9)
+    traffic = ncu_traffic()
+    cpu = None
+    if not args.no_cpu_baseline:
+        gcpu, threads, n, dt = cpu_sssp(off, dst, w, sources, delta, 15.0)
+        cpu = {"value": gcpu, "unit": "GTEPS", "cores": threads, "kind": "port",
+               "sample": f"{n} of the {N_SOURCES} sources ({dt:.1f} s), GAPBS "
+                         f"OrderedProcessingOperatorNoMerge port, same graph and delta"}
+    out = {
+        "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": f"sssp_delta_stepping_rmat{args.scale}_k16_directed",
+                   "V": V, "E": E, "sources": N_SOURCES, "delta": delta,
+                   "weights": "U[1,255]", "schedule": "PUSH SPARSE VERTEX_BASED fused (sssp.cpp default)",
+                   "mode": "plain single-source", "l2": "inputs larger than L2 (CSR %.2f GB)"
+                   % ((off.nbytes + dst.nbytes + w.nbytes) / 1e9),
+                   "parallelism": f"replicas x{world}, sources by rank"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "k_sssp_fused<VERTEX_BASED>",
+                     "peak_kind": peak_kind,
+                     "bytes_model": "12*E_r + 16*V_r per source"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_val, "unit": "GTEPS", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+    }
+    print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

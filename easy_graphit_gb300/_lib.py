@@ -52,7 +52,7 @@ class gg_vertex_data(C.Structure):
 class gg_stats(C.Structure):
     _fields_ = [("iterations", i32), ("push_iterations", i32), ("pull_iterations", i32),
                 ("bucket_advances", i32), ("vertices_reached", i64), ("edges_traversed", i64),
-                ("device_ms", f32)]
+                ("device_ms", f32), ("loop_ms", f32), ("fused", i32), ("launches", i32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -71,6 +71,7 @@ SIGNATURES: dict[str, tuple] = {
     "gg_host_graph_load": (i32, [C.c_char_p, i32, C.POINTER(P)]),
     "gg_host_graph_save_bin": (i32, [P, C.c_char_p]),
     "gg_host_graph_info": (i32, [P, Pi32, C.POINTER(i64)]),
+    "gg_host_graph_pick_sources": (i32, [P, i32, i64, P]),
     "gg_host_graph_offsets": (P, [P]),
     "gg_host_graph_dst": (P, [P]),
     "gg_host_graph_weights": (P, [P]),
@@ -112,6 +113,7 @@ SIGNATURES: dict[str, tuple] = {
     "gg_cc": (i32, [P, C.POINTER(gg_app_schedule), P, C.POINTER(gg_stats)]),
     "gg_bc": (i32, [P, C.POINTER(gg_app_schedule), i32, P, C.POINTER(gg_stats)]),
     "gg_debug_barrier_timeout": (i32, [i32]),
+    "gg_kernel_launches": (C.c_uint64, []),
 }
 
 _lib = None

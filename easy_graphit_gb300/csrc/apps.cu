@@ -75,7 +75,7 @@ gg_status reach_stats(gg_graph *g, const int32_t *val, gg_stats *st) {
   if (!st) return GG_OK;
   unsigned long long *d = reinterpret_cast<unsigned long long *>(g->d_misc + 32);
   GG_CUDA(cudaMemsetAsync(d, 0, 16, g->stream));
-  k_reach<<<g->sm_count * 4, 256, 0, g->stream>>>(val, g->csr.off, g->csr.V, d);
+  { gg::note_launch(); k_reach<<<g->sm_count * 4, 256, 0, g->stream>>>(val, g->csr.off, g->csr.V, d); }
   GG_CUDA(cudaGetLastError());
   unsigned long long h[2];
   GG_CUDA(cudaMemcpyAsync(h, d, 16, cudaMemcpyDeviceToHost, g->stream));
@@ -85,14 +85,34 @@ gg_status reach_stats(gg_graph *g, const int32_t *val, gg_stats *st) {
   return GG_OK;
 }
 
+// CUDA events around one trial (and, when a loop recorded ev2/ev3, around its
+// traversal loop), plus the number of kernels the trial launched.
 struct Trial {
   gg_graph *g;
-  explicit Trial(gg_graph *gr) : g(gr) { cudaEventRecord(g->ev0, g->stream); }
+  uint64_t l0;
+  explicit Trial(gg_graph *gr) : g(gr), l0(launches()) {
+    g->loop_timed = false;
+    cudaEventRecord(g->ev0, g->stream);
+  }
   gg_status stop(gg_stats *st) {
     GG_CUDA(cudaEventRecord(g->ev1, g->stream));
     GG_CUDA(cudaEventSynchronize(g->ev1));
-    if (st) GG_CUDA(cudaEventElapsedTime(&st->device_ms, g->ev0, g->ev1));
+    if (st) {
+      GG_CUDA(cudaEventElapsedTime(&st->device_ms, g->ev0, g->ev1));
+      if (g->loop_timed) GG_CUDA(cudaEventElapsedTime(&st->loop_ms, g->ev2, g->ev3));
+      st->launches = (int32_t)(launches() - l0);
+    }
     return GG_OK;
+  }
+};
+
+// Brackets an unfused traversal loop with ev2/ev3.
+struct LoopTimer {
+  gg_graph *g;
+  explicit LoopTimer(gg_graph *gr) : g(gr) { cudaEventRecord(g->ev2, g->stream); }
+  ~LoopTimer() {
+    cudaEventRecord(g->ev3, g->stream);
+    g->loop_timed = true;
   }
 };
 
@@ -145,10 +165,12 @@ gg_status run_bfs(gg_graph *g, const gg_app_schedule *s, int32_t src, int32_t *p
       if (st) {
         st->iterations = iters;
         st->push_iterations = iters;
+        st->fused = 1;
       }
       return check_device_error(g, "bfs");
     }
   }
+  LoopTimer lt(g);
   int32_t n = 1;
   for (int32_t level = 1;; ++level) {
     GG_TRY(frontier_size(f, &n));
@@ -185,10 +207,12 @@ gg_status run_sssp(gg_graph *g, const gg_app_schedule *s, int32_t src, int32_t d
         st->iterations = iters;
         st->push_iterations = iters;
         st->bucket_advances = (int32_t)adv;
+        st->fused = 1;
       }
       return check_device_error(g, "sssp");
     }
   }
+  LoopTimer lt(g);
   const int32_t V = g->csr.V;
   for (;;) {
     bool fin = false;
@@ -392,7 +416,7 @@ gg_status gg_bc(gg_graph *g, const gg_app_schedule *s, int32_t src, float *dep_o
     st->iterations = levels;
     int32_t *tmp = nullptr;
     GG_TRY(app_array(g, 0, V, &tmp));
-    k_sigma_to_reach<<<g->sm_count * 4, 256, 0, g->stream>>>(sigma, V, tmp);
+    { gg::note_launch(); k_sigma_to_reach<<<g->sm_count * 4, 256, 0, g->stream>>>(sigma, V, tmp); }
     GG_CUDA(cudaGetLastError());
     GG_TRY(reach_stats(g, tmp, st));
     st->edges_traversed *= 2;  // forward + backward sweeps

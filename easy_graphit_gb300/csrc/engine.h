@@ -41,7 +41,9 @@ struct gg_graph {
   uint32_t *d_bar = nullptr;      // grid barrier state [2]
   int32_t *d_misc = nullptr;      // small device scratch (counters, flags), 64 ints
   int32_t *h_pinned = nullptr;    // pinned host scratch, 64 ints
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // whole trial
+  cudaEvent_t ev2 = nullptr, ev3 = nullptr;  // traversal loop
+  bool loop_timed = false;                   // ev2/ev3 bracket the last loop
   int sm_count = 0;
   int device = 0;
   gg::Scratch scratch[4];         // LB scratch (TWC bins, STRICT sums, ETWC chunks)

@@ -1,6 +1,7 @@
 // Thread-local error reporting for the C ABI.  The reference prints and calls
 // exit(-1) (runtime/infra_gpu/support.h:4-10); here the status is returned and
 // the message is kept for gg_last_error().
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 
@@ -25,7 +26,13 @@ gg_status set_error(gg_status s, const char *fmt, ...) {
 
 void clear_error() { t_last_error.clear(); }
 
+static std::atomic<uint64_t> g_launch_count{0};
+void note_launch() { g_launch_count.fetch_add(1, std::memory_order_relaxed); }
+uint64_t launches() { return g_launch_count.load(std::memory_order_relaxed); }
+
 }  // namespace gg
+
+extern "C" uint64_t gg_kernel_launches(void) { return gg::launches(); }
 
 extern "C" size_t gg_last_error(char *buf, size_t n) {
   const std::string &e = gg::t_last_error;

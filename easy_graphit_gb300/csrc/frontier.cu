@@ -328,9 +328,9 @@ gg_status frontier_prepare_sparse(gg_frontier *f) {
   cudaStream_t st = g->stream;
   GG_CUDA(cudaMemsetAsync(f->cnt_out, 0, sizeof(int32_t), st));
   if (f->fmt == GG_FMT_BITMAP)
-    k_bitmap_to_sparse<<<grid_of(g), kThreads, 0, st>>>(f->bm_in, f->nwords, f->V, f->q_out, f->cnt_out);
+    { gg::note_launch(); k_bitmap_to_sparse<<<grid_of(g), kThreads, 0, st>>>(f->bm_in, f->nwords, f->V, f->q_out, f->cnt_out); }
   else
-    k_boolmap_to_sparse<<<grid_of(g), kThreads, 0, st>>>(f->by_in, f->V, f->q_out, f->cnt_out);
+    { gg::note_launch(); k_boolmap_to_sparse<<<grid_of(g), kThreads, 0, st>>>(f->by_in, f->V, f->q_out, f->cnt_out); }
   GG_CUDA(cudaGetLastError());
   std::swap(f->q_in, f->q_out);
   swap_counts(f);
@@ -345,9 +345,9 @@ gg_status frontier_prepare_bitmap(gg_frontier *f) {
   GG_CUDA(cudaMemsetAsync(f->cnt_out, 0, sizeof(int32_t), st));
   if (f->fmt == GG_FMT_SPARSE) {
     GG_CUDA(cudaMemsetAsync(f->bm_out, 0, sizeof(uint32_t) * f->nwords, st));
-    k_sparse_to_bitmap<<<grid_of(g), kThreads, 0, st>>>(f->q_in, f->cnt_in, f->bm_out, f->cnt_out);
+    { gg::note_launch(); k_sparse_to_bitmap<<<grid_of(g), kThreads, 0, st>>>(f->q_in, f->cnt_in, f->bm_out, f->cnt_out); }
   } else {
-    k_boolmap_to_bitmap<<<grid_of(g), kThreads, 0, st>>>(f->by_in, f->nwords, f->V, f->bm_out, f->cnt_out);
+    { gg::note_launch(); k_boolmap_to_bitmap<<<grid_of(g), kThreads, 0, st>>>(f->by_in, f->nwords, f->V, f->bm_out, f->cnt_out); }
   }
   GG_CUDA(cudaGetLastError());
   std::swap(f->bm_in, f->bm_out);
@@ -363,9 +363,9 @@ gg_status frontier_prepare_boolmap(gg_frontier *f) {
   GG_CUDA(cudaMemsetAsync(f->cnt_out, 0, sizeof(int32_t), st));
   if (f->fmt == GG_FMT_SPARSE) {
     GG_CUDA(cudaMemsetAsync(f->by_out, 0, f->bytes_padded, st));
-    k_sparse_to_boolmap<<<grid_of(g), kThreads, 0, st>>>(f->q_in, f->cnt_in, f->by_out, f->cnt_out);
+    { gg::note_launch(); k_sparse_to_boolmap<<<grid_of(g), kThreads, 0, st>>>(f->q_in, f->cnt_in, f->by_out, f->cnt_out); }
   } else {
-    k_bitmap_to_boolmap<<<grid_of(g), kThreads, 0, st>>>(f->bm_in, f->nwords, f->V, f->by_out, f->cnt_out);
+    { gg::note_launch(); k_bitmap_to_boolmap<<<grid_of(g), kThreads, 0, st>>>(f->bm_in, f->nwords, f->V, f->by_out, f->cnt_out); }
   }
   GG_CUDA(cudaGetLastError());
   std::swap(f->by_in, f->by_out);
@@ -434,7 +434,7 @@ gg_status frontier_dedup(gg_frontier *f) {
   cudaStream_t st = g->stream;
   f->epoch++;
   GG_CUDA(cudaMemsetAsync(f->cnt_out, 0, sizeof(int32_t), st));
-  k_dedup<<<grid_of(g), kThreads, 0, st>>>(f->q_in, f->cnt_in, f->dedup, f->epoch, f->q_out, f->cnt_out);
+  { gg::note_launch(); k_dedup<<<grid_of(g), kThreads, 0, st>>>(f->q_in, f->cnt_in, f->dedup, f->epoch, f->q_out, f->cnt_out); }
   GG_CUDA(cudaGetLastError());
   std::swap(f->q_in, f->q_out);
   swap_counts(f);
@@ -448,7 +448,7 @@ gg_status reverse_frontier(gg_graph *g, int32_t filter, const VData &vd, int32_t
   *q = (int32_t *)p;
   *cnt = *q + V + 16;
   GG_CUDA(cudaMemsetAsync(*cnt, 0, sizeof(int32_t), g->stream));
-  k_reverse<<<grid_of(g), kThreads, 0, g->stream>>>(filter, vd, V, *q, *cnt);
+  { gg::note_launch(); k_reverse<<<grid_of(g), kThreads, 0, g->stream>>>(filter, vd, V, *q, *cnt); }
   GG_CUDA(cudaGetLastError());
   return GG_OK;
 }
@@ -461,7 +461,7 @@ gg_status twc_bin(gg_graph *G, const DGraph &g, const Enum &en, int32_t n_host, 
   *bins = (int32_t *)p;
   *bin_cnt = *bins + 3 * cap + 4;
   GG_CUDA(cudaMemsetAsync(*bin_cnt, 0, sizeof(int32_t) * 3, G->stream));
-  k_twc_bin<<<grid_of(G), kThreads, 0, G->stream>>>(g, en, cta, *bins, cap, *bin_cnt);
+  { gg::note_launch(); k_twc_bin<<<grid_of(G), kThreads, 0, G->stream>>>(g, en, cta, *bins, cap, *bin_cnt); }
   GG_CUDA(cudaGetLastError());
   return GG_OK;
 }
@@ -515,7 +515,7 @@ gg_status vertexset_apply_impl(gg_graph *g, gg_frontier *set, int32_t vudf, cons
   }
   const float beta = (float)((1.0 - (double)vd.damping) / V);
   const float inv_v = (float)(1.0 / V);
-  k_vertexset<<<grid_of(g), kThreads, 0, g->stream>>>(vudf, vd, q, n_dev, V, g->csr.off, beta, inv_v);
+  { gg::note_launch(); k_vertexset<<<grid_of(g), kThreads, 0, g->stream>>>(vudf, vd, q, n_dev, V, g->csr.off, beta, inv_v); }
   GG_CUDA(cudaGetLastError());
   return GG_OK;
 }
@@ -538,7 +538,7 @@ gg_status gg_frontier_create(gg_graph *g, int32_t init_all, gg_frontier **out) {
     return s;
   }
   if (init_all) {  // create_new_vertex_set(V, V): initialize_frontier_all
-    k_iota<<<grid_of(g), kThreads, 0, g->stream>>>(f->q_in, f->V, f->cnt_in);
+    { gg::note_launch(); k_iota<<<grid_of(g), kThreads, 0, g->stream>>>(f->q_in, f->V, f->cnt_in); }
     GG_CUDA(cudaGetLastError());
   }
   GG_CUDA(cudaStreamSynchronize(g->stream));
@@ -578,9 +578,9 @@ gg_status gg_frontier_add(gg_frontier *f, int32_t v) {
     int32_t *one = g->d_misc + 8;
     GG_CUDA(cudaMemcpyAsync(one, g->h_pinned + 1, sizeof(int32_t) * 2, cudaMemcpyHostToDevice, st));
     if (f->fmt == GG_FMT_BITMAP)
-      k_sparse_to_bitmap<<<1, 32, 0, st>>>(one, one + 1, f->bm_in, f->cnt_in);
+      { gg::note_launch(); k_sparse_to_bitmap<<<1, 32, 0, st>>>(one, one + 1, f->bm_in, f->cnt_in); }
     else
-      k_sparse_to_boolmap<<<1, 32, 0, st>>>(one, one + 1, f->by_in, f->cnt_in);
+      { gg::note_launch(); k_sparse_to_boolmap<<<1, 32, 0, st>>>(one, one + 1, f->by_in, f->cnt_in); }
     GG_CUDA(cudaGetLastError());
   }
   GG_CUDA(cudaStreamSynchronize(st));

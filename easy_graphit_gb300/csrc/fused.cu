@@ -187,7 +187,11 @@ static gg_status coop_launch(gg_graph *g, K kernel, int cta, size_t smem, FusedA
   const int grid = per_sm * g->sm_count;
   GG_CUDA(cudaMemsetAsync(g->d_bar, 0, sizeof(uint32_t) * 2, g->stream));
   void *args[] = {&a};
+  GG_CUDA(cudaEventRecord(g->ev2, g->stream));
+  note_launch();
   GG_CUDA(cudaLaunchCooperativeKernel((const void *)kernel, grid, cta, args, smem, g->stream));
+  GG_CUDA(cudaEventRecord(g->ev3, g->stream));
+  g->loop_timed = true;
   return GG_OK;
 }
 
@@ -295,7 +299,7 @@ extern "C" gg_status gg_debug_barrier_timeout(int32_t timeout_us) {
   GG_CUDA(cudaMalloc(&err, sizeof(int32_t)));
   GG_CUDA(cudaMemset(bar, 0, sizeof(uint32_t) * 2));
   GG_CUDA(cudaMemset(err, 0, sizeof(int32_t)));
-  k_barrier_never<<<2, 32>>>(bar, err, (uint64_t)timeout_us * 1000ull);
+  { gg::note_launch(); k_barrier_never<<<2, 32>>>(bar, err, (uint64_t)timeout_us * 1000ull); }
   cudaError_t le = cudaGetLastError();
   cudaError_t se = cudaDeviceSynchronize();
   int32_t h = 0;

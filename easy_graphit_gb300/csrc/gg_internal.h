@@ -19,6 +19,10 @@ void clear_error();
 extern int32_t g_default_max_cta;
 extern int32_t g_default_cta_size;
 
+// Counts kernel launches issued by the library (gg_kernel_launches()).
+void note_launch();
+uint64_t launches();
+
 }  // namespace gg
 
 // The host CSR graph (gg_host_graph in the ABI).

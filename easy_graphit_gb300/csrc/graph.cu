@@ -200,7 +200,7 @@ gg_status ensure_coo(GraphStore &s, cudaStream_t st) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  k_coo_src<<<sms * 8, 256, 0, st>>>(s.off, s.V, s.E, s.src);
+  { gg::note_launch(); k_coo_src<<<sms * 8, 256, 0, st>>>(s.off, s.V, s.E, s.src); }
   GG_CUDA(cudaGetLastError());
   return GG_OK;
 }
@@ -229,13 +229,13 @@ gg_status ensure_transpose(gg_graph *g) {
   GG_CUDA(cudaMallocAsync(&partial, sizeof(int32_t) * scan_scratch_ints(f.V), st));
   GG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (f.V + 1), st));
   const int grid = stream_grid(g);
-  k_count_dst<<<grid, 256, 0, st>>>(f.dst, f.E, cnt);
+  { gg::note_launch(); k_count_dst<<<grid, 256, 0, st>>>(f.dst, f.E, cnt); }
   GG_CUDA(exclusive_scan(ArrIn{cnt}, f.V, t->off, partial, st));
   GG_CUDA(cudaMemcpyAsync(cnt, t->off, sizeof(int32_t) * f.V, cudaMemcpyDeviceToDevice, st));
-  k_transpose_scatter<<<grid, 256, 0, st>>>(g->csr.src, f.dst, f.w, f.E, cnt, t->dst, t->w, t->src);
+  { gg::note_launch(); k_transpose_scatter<<<grid, 256, 0, st>>>(g->csr.src, f.dst, f.w, f.E, cnt, t->dst, t->w, t->src); }
   GG_CUDA(cudaGetLastError());
   // Deterministic in-lists.
-  k_sort_lists<<<grid, 256, 0, st>>>(t->off, t->V, t->dst, t->w);
+  { gg::note_launch(); k_sort_lists<<<grid, 256, 0, st>>>(t->off, t->V, t->dst, t->w); }
   GG_CUDA(cudaGetLastError());
   // Lists longer than the shared-memory tile (hubs): bitonic in global memory.
   std::vector<int32_t> hoff(t->V + 1);
@@ -263,11 +263,11 @@ gg_status ensure_transpose(gg_graph *g) {
     GG_CUDA(cudaMemcpyAsync(ids, longs.data(), sizeof(int32_t) * nl, cudaMemcpyHostToDevice, st));
     GG_CUDA(cudaMemcpyAsync(dpoff, poff.data(), sizeof(int64_t) * (nl + 1), cudaMemcpyHostToDevice, st));
     dim3 grd((unsigned)std::min<int64_t>(64, (maxp2 + 255) / 256), (unsigned)std::min(nl, 1024));
-    k_long_copy_in<<<grd, 256, 0, st>>>(t->off, ids, dpoff, nl, t->dst, t->w, tk, tw);
+    { gg::note_launch(); k_long_copy_in<<<grd, 256, 0, st>>>(t->off, ids, dpoff, nl, t->dst, t->w, tk, tw); }
     for (int64_t k = 2; k <= maxp2; k <<= 1)
       for (int64_t j = k >> 1; j > 0; j >>= 1)
-        k_long_step<<<grd, 256, 0, st>>>(dpoff, nl, tk, tw, k, j);
-    k_long_copy_out<<<grd, 256, 0, st>>>(t->off, ids, dpoff, nl, t->dst, t->w, tk, tw);
+        { gg::note_launch(); k_long_step<<<grd, 256, 0, st>>>(dpoff, nl, tk, tw, k, j); }
+    { gg::note_launch(); k_long_copy_out<<<grd, 256, 0, st>>>(t->off, ids, dpoff, nl, t->dst, t->w, tk, tw); }
     GG_CUDA(cudaGetLastError());
     GG_CUDA(cudaStreamSynchronize(st));
     for (void *p : {(void *)ids, (void *)dpoff, (void *)tk, (void *)tw}) cudaFreeAsync(p, st);
@@ -306,11 +306,11 @@ gg_status ensure_blocked(gg_graph *g, bool reverse, int32_t block_size, const Gr
   GG_CUDA(cudaMallocAsync(&partial, sizeof(int32_t) * scan_scratch_ints(b.nbuckets), st));
   GG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (b.nbuckets + 1), st));
   const int grid = stream_grid(g);
-  k_bucket_count<<<grid, 256, 0, st>>>(base.dst, base.E, block_size, cnt);
+  { gg::note_launch(); k_bucket_count<<<grid, 256, 0, st>>>(base.dst, base.E, block_size, cnt); }
   GG_CUDA(exclusive_scan(ArrIn{cnt}, b.nbuckets, b.bucket, partial, st));
   GG_CUDA(cudaMemcpyAsync(cnt, b.bucket, sizeof(int32_t) * b.nbuckets, cudaMemcpyDeviceToDevice, st));
-  k_bucket_scatter<<<grid, 256, 0, st>>>(base.src, base.dst, base.w, base.E, block_size, cnt, b.src,
-                                         b.dst, b.w);
+  { gg::note_launch(); k_bucket_scatter<<<grid, 256, 0, st>>>(base.src, base.dst, base.w, base.E, block_size, cnt, b.src,
+                                         b.dst, b.w); }
   GG_CUDA(cudaGetLastError());
   cudaFreeAsync(cnt, st);
   cudaFreeAsync(partial, st);
@@ -397,6 +397,8 @@ gg_status gg_graph_create(const int32_t *offsets, const int32_t *dst, const int3
   GG_CUDA(cudaMallocHost(&g->h_pinned, sizeof(int32_t) * 64));
   GG_CUDA(cudaEventCreate(&g->ev0));
   GG_CUDA(cudaEventCreate(&g->ev1));
+  GG_CUDA(cudaEventCreate(&g->ev2));
+  GG_CUDA(cudaEventCreate(&g->ev3));
   GG_TRY(ensure_coo(s, st));
   GG_CUDA(cudaStreamSynchronize(st));
   *out = g.release();
@@ -423,6 +425,8 @@ gg_status gg_graph_destroy(gg_graph *g) {
   if (g->h_pinned) cudaFreeHost(g->h_pinned);
   if (g->ev0) cudaEventDestroy(g->ev0);
   if (g->ev1) cudaEventDestroy(g->ev1);
+  if (g->ev2) cudaEventDestroy(g->ev2);
+  if (g->ev3) cudaEventDestroy(g->ev3);
   if (g->own_stream) cudaStreamDestroy(g->own_stream);
   delete g;
   return GG_OK;

@@ -446,6 +446,23 @@ gg_status gg_host_graph_save_bin(const gg_host_graph *g, const char *path) {
   return GG_OK;
 }
 
+gg_status gg_host_graph_pick_sources(const gg_host_graph *g, int32_t n, int64_t seed, int32_t *out) {
+  GG_CHECK_ARG(g && out && n >= 0, "bad arguments");
+  if (g->E == 0) return gg::set_error(GG_ERR_INVALID, "graph has no edges to pick sources from");
+  // SourcePicker::PickNext (infra_gapbs/benchmark.h:50-71): uniform ids from one
+  // std::mt19937, rejecting vertices without out-edges.
+  std::mt19937 rng((std::mt19937::result_type)seed);
+  std::uniform_int_distribution<int32_t> udist(0, g->V - 1);
+  for (int32_t i = 0; i < n; ++i) {
+    int32_t s;
+    do {
+      s = udist(rng);
+    } while (g->offsets[s + 1] == g->offsets[s]);
+    out[i] = s;
+  }
+  return GG_OK;
+}
+
 gg_status gg_host_graph_info(const gg_host_graph *g, int32_t *num_vertices, int64_t *num_edges) {
   GG_CHECK_ARG(g, "graph is NULL");
   if (num_vertices) *num_vertices = g->V;

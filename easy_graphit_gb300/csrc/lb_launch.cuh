@@ -107,29 +107,29 @@ gg_status launch_lb(const EdgeLaunch &L, const F &f) {
     case GG_LB_EDGE_ONLY: {
       if (L.g.nbuckets > 0) {
         auto k = k_edge_only_blocked<F>;
-        k<<<grid_for(k, cta, 0, sms, -1), cta, 0, st>>>(L.g, f, L.out);
+        { gg::note_launch(); k<<<grid_for(k, cta, 0, sms, -1), cta, 0, st>>>(L.g, f, L.out); }
       } else {
         auto k = k_edge_only<F>;
-        k<<<grid_for(k, cta, 0, sms, -1), cta, 0, st>>>(L.g, f, L.out);
+        { gg::note_launch(); k<<<grid_for(k, cta, 0, sms, -1), cta, 0, st>>>(L.g, f, L.out); }
       }
       break;
     }
     case GG_LB_VERTEX_BASED: {
       auto k = k_vertex<F>;
-      k<<<grid_for(k, cta, 0, sms, n < 0 ? -1 : ceil_div(n, cta)), cta, 0, st>>>(L.g, L.en, f, L.out);
+      { gg::note_launch(); k<<<grid_for(k, cta, 0, sms, n < 0 ? -1 : ceil_div(n, cta)), cta, 0, st>>>(L.g, L.en, f, L.out); }
       break;
     }
     case GG_LB_WM: {
       auto k = k_wm<F>;
-      k<<<grid_for(k, cta, 0, sms, n < 0 ? -1 : ceil_div(n, cta / 32)), cta, 0, st>>>(L.g, L.en, f,
-                                                                                     L.out);
+      { gg::note_launch(); k<<<grid_for(k, cta, 0, sms, n < 0 ? -1 : ceil_div(n, cta / 32)), cta, 0, st>>>(L.g, L.en, f,
+                                                                                     L.out); }
       break;
     }
     case GG_LB_TWCE: {
       auto k = k_twce<F, true>;
       const size_t sm = twce_smem_bytes(cta);
-      k<<<grid_for(k, cta, sm, sms, n < 0 ? -1 : ceil_div(n, cta / kStage1)), cta, sm, st>>>(
-          L.g, L.en, f, L.out, nullptr, nullptr, 0);
+      { gg::note_launch(); k<<<grid_for(k, cta, sm, sms, n < 0 ? -1 : ceil_div(n, cta / kStage1)), cta, sm, st>>>(
+          L.g, L.en, f, L.out, nullptr, nullptr, 0); }
       break;
     }
     case GG_LB_ETWC: {
@@ -141,17 +141,17 @@ gg_status launch_lb(const EdgeLaunch &L, const F &f) {
       GG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t), st));
       auto k = k_twce<F, false>;
       const size_t sm = twce_smem_bytes(cta);
-      k<<<grid_for(k, cta, sm, sms, n < 0 ? -1 : ceil_div(n, cta / kStage1)), cta, sm, st>>>(
-          L.g, L.en, f, L.out, chunks, cnt, chunk);
+      { gg::note_launch(); k<<<grid_for(k, cta, sm, sms, n < 0 ? -1 : ceil_div(n, cta / kStage1)), cta, sm, st>>>(
+          L.g, L.en, f, L.out, chunks, cnt, chunk); }
       auto k2 = k_chunks<F>;
-      k2<<<grid_for(k2, cta, 0, sms, -1), cta, 0, st>>>(L.g, chunks, cnt, f, L.out);
+      { gg::note_launch(); k2<<<grid_for(k2, cta, 0, sms, -1), cta, 0, st>>>(L.g, chunks, cnt, f, L.out); }
       break;
     }
     case GG_LB_CM: {
       auto k = k_cm<F>;
       const size_t sm = cm_smem_bytes(cta);
-      k<<<grid_for(k, cta, sm, sms, n < 0 ? -1 : ceil_div(n, cta)), cta, sm, st>>>(L.g, L.en, f,
-                                                                                  L.out);
+      { gg::note_launch(); k<<<grid_for(k, cta, sm, sms, n < 0 ? -1 : ceil_div(n, cta)), cta, sm, st>>>(L.g, L.en, f,
+                                                                                  L.out); }
       break;
     }
     case GG_LB_TWC: {
@@ -163,16 +163,16 @@ gg_status launch_lb(const EdgeLaunch &L, const F &f) {
       auto k1 = k_vertex<F>;
       auto k2 = k_wm<F>;
       auto k3 = k_cta<F>;
-      k1<<<grid_for(k1, cta, 0, sms, -1), cta, 0, st>>>(L.g, small, f, L.out);
-      k2<<<grid_for(k2, cta, 0, sms, -1), cta, 0, st>>>(L.g, mid, f, L.out);
-      k3<<<grid_for(k3, cta, 0, sms, -1), cta, 0, st>>>(L.g, large, f, L.out);
+      { gg::note_launch(); k1<<<grid_for(k1, cta, 0, sms, -1), cta, 0, st>>>(L.g, small, f, L.out); }
+      { gg::note_launch(); k2<<<grid_for(k2, cta, 0, sms, -1), cta, 0, st>>>(L.g, mid, f, L.out); }
+      { gg::note_launch(); k3<<<grid_for(k3, cta, 0, sms, -1), cta, 0, st>>>(L.g, large, f, L.out); }
       break;
     }
     case GG_LB_STRICT: {
       int32_t *sum = nullptr;
       GG_TRY(strict_scan(G, L.g, L.en, (int32_t)n, &sum));
       auto k = k_strict<F>;
-      k<<<grid_for(k, cta, 0, sms, -1), cta, 0, st>>>(L.g, L.en, sum, f, L.out, 8 * cta);
+      { gg::note_launch(); k<<<grid_for(k, cta, 0, sms, -1), cta, 0, st>>>(L.g, L.en, sum, f, L.out, 8 * cta); }
       break;
     }
     default:

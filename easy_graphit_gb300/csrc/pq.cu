@@ -76,7 +76,7 @@ gg_status pq_advance(gg_pq *pq) {
   GG_CUDA(cudaMemcpyAsync(gmin, g->h_pinned + 5, sizeof(int32_t), cudaMemcpyHostToDevice, st));
   const int grid = g->sm_count * 4;
   if (pq->window_upper < INT_MAX)
-    k_pq_min<<<grid, kPqThreads, 0, st>>>(pq->prio, V, (int32_t)pq->window_upper, gmin);
+    { gg::note_launch(); k_pq_min<<<grid, kPqThreads, 0, st>>>(pq->prio, V, (int32_t)pq->window_upper, gmin); }
   GG_CUDA(cudaGetLastError());
   GG_CUDA(cudaMemcpyAsync(g->h_pinned + 6, gmin, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   GG_CUDA(cudaStreamSynchronize(st));
@@ -84,8 +84,8 @@ gg_status pq_advance(gg_pq *pq) {
   gg_frontier *f = pq->frontier;
   GG_CUDA(cudaMemsetAsync(f->cnt_out, 0, sizeof(int32_t), st));
   if (pq->cur != INT_MAX)
-    k_pq_bucket<<<grid, kPqThreads, 0, st>>>(pq->prio, V, (int32_t)pq->cur, pq->cur + pq->delta,
-                                             f->q_out, f->cnt_out);
+    { gg::note_launch(); k_pq_bucket<<<grid, kPqThreads, 0, st>>>(pq->prio, V, (int32_t)pq->cur, pq->cur + pq->delta,
+                                             f->q_out, f->cnt_out); }
   GG_CUDA(cudaGetLastError());
   std::swap(f->q_in, f->q_out);
   std::swap(f->cnt_in, f->cnt_out);

@@ -82,9 +82,9 @@ template <class In>
 cudaError_t exclusive_scan(In in, int64_t n, int32_t *out, int32_t *partial, cudaStream_t st) {
   if (n <= 0) return cudaMemsetAsync(out, 0, sizeof(int32_t), st);
   const int32_t nb = (int32_t)((n + kScanTile - 1) / kScanTile);
-  k_scan_tiles<In><<<nb, kScanThreads, 0, st>>>(in, n, partial);
-  k_scan_partials<<<1, 1024, 0, st>>>(partial, nb);
-  k_scan_apply<In><<<nb, kScanThreads, 0, st>>>(in, n, partial, out);
+  { gg::note_launch(); k_scan_tiles<In><<<nb, kScanThreads, 0, st>>>(in, n, partial); }
+  { gg::note_launch(); k_scan_partials<<<1, 1024, 0, st>>>(partial, nb); }
+  { gg::note_launch(); k_scan_apply<In><<<nb, kScanThreads, 0, st>>>(in, n, partial, out); }
   return cudaGetLastError();
 }
 

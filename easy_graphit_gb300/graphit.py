@@ -277,6 +277,12 @@ class HostGraph:
     def out_degrees(self) -> np.ndarray:
         return np.diff(self.offsets)
 
+    def pick_sources(self, n: int, seed: int = K_RAND_SEED) -> np.ndarray:
+        """GAPBS SourcePicker (benchmark.h:50-71): n non-zero-degree vertices."""
+        out = np.empty(n, dtype=np.int32)
+        call("gg_host_graph_pick_sources", self._h, n, seed, _np_ptr(out))
+        return out
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h and lib is not None:

@@ -137,6 +137,10 @@ gg_status gg_host_graph_load(const char *path, int32_t symmetrize,
 gg_status gg_host_graph_save_bin(const gg_host_graph *g, const char *path);
 gg_status gg_host_graph_info(const gg_host_graph *g, int32_t *num_vertices,
                              int64_t *num_edges);
+/* n sources as GAPBS's SourcePicker draws them (infra_gapbs/benchmark.h:50-71):
+ * uniform ids from std::mt19937(seed), skipping vertices with no out-edges. */
+gg_status gg_host_graph_pick_sources(const gg_host_graph *g, int32_t n,
+                                     int64_t seed, int32_t *out);
 const int32_t *gg_host_graph_offsets(const gg_host_graph *g);
 const int32_t *gg_host_graph_dst(const gg_host_graph *g);
 const int32_t *gg_host_graph_weights(const gg_host_graph *g);
@@ -282,7 +286,14 @@ typedef struct gg_stats {
   int64_t vertices_reached;
   int64_t edges_traversed;  /* algorithmic edges: sum of out-degree of reached v   */
   float device_ms;          /* CUDA-event time of the trial on the graph's stream  */
+  float loop_ms;            /* CUDA-event time of the traversal loop alone (the
+                               fused kernel, or the unfused iterations)            */
+  int32_t fused;            /* 1 when the loop ran as one persistent kernel        */
+  int32_t launches;         /* kernels this call launched                           */
 } gg_stats;
+
+/* Number of kernels libgg.so has launched in this process. */
+uint64_t gg_kernel_launches(void);
 
 /* BFS from src: depth_out[v] = hop distance (-1 unreached); parent_out (may be
  * NULL) = the parent array of bfs.cpp (parent[src] = src). */

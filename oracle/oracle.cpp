@@ -235,7 +235,9 @@ void orc_sssp_ordered(int32_t V, const int32_t *off, const int32_t *dst,
 #pragma omp parallel for schedule(static)
   for (int32_t v = 0; v < V; ++v) P[v].store(INT_MAX, std::memory_order_relaxed);
   P[src].store(0);
-  std::vector<int32_t> frontier((size_t)std::max<int64_t>(off[V], 1) + 1);
+  // Bins persist across rounds, so a round's frontier can exceed E; size for
+  // E + V entries twice over.
+  std::vector<int32_t> frontier(2 * ((size_t)off[V] + (size_t)V) + 1);
   size_t shared_indexes[2] = {0, kMaxBin};
   std::atomic<size_t> frontier_tails[2];
   frontier_tails[0] = 1;
