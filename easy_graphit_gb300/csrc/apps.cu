@@ -361,8 +361,10 @@ gg_status gg_bc(gg_graph *g, const gg_app_schedule *s, int32_t src, float *dep_o
   double *sigma = nullptr;
   float *dep = nullptr;
   uint8_t *visited = nullptr;
+  double *dep64 = nullptr;
   GG_TRY(app_array(g, 6, V, &sigma));
   GG_TRY(app_array(g, 5, V, &dep));
+  GG_TRY(app_array(g, 3, V, &dep64));
   GG_TRY(app_array(g, 7, V, &visited));
   gg_frontier *f = nullptr;
   GG_TRY(app_frontier(g, &f));
@@ -372,6 +374,9 @@ gg_status gg_bc(gg_graph *g, const gg_app_schedule *s, int32_t src, float *dep_o
   VData vd{};
   vd.num_paths = sigma;
   vd.dependences = dep;
+  // fp32 atomic accumulation (the reference's float dependences) drifts past
+  // 1e-6 relative L1 on R-MAT hubs; accumulate in fp64, store fp32 at the end.
+  vd.dep64 = dep64;
   vd.visited = visited;
   vd.src = src;
   Trial t(g);

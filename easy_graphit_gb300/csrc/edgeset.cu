@@ -37,7 +37,7 @@ static gg_status check_udf(int32_t udf, const VData &vd) {
     case GG_UDF_PR_ADD: ok = vd.contrib && vd.new_rank; break;
     case GG_UDF_CC_HOOK: ok = vd.ids && vd.updates; break;
     case GG_UDF_BC_FORWARD: ok = vd.num_paths && vd.visited; break;
-    case GG_UDF_BC_BACKWARD: ok = vd.dependences && vd.visited; break;
+    case GG_UDF_BC_BACKWARD: ok = (vd.dependences || vd.dep64) && vd.visited; break;
     default: return set_error(GG_ERR_INVALID, "unknown edge UDF %d", udf);
   }
   if (!ok) return set_error(GG_ERR_INVALID, "vertex data needed by UDF %d is NULL", udf);

@@ -5,7 +5,11 @@
 namespace gg {
 
 gg_status launch_bcb(const EdgeLaunch &L) {
-  UBcB u{L.vd.dependences, L.vd.visited};
+  if (L.vd.dep64) {
+    UBcB<double> u{L.vd.dep64, L.vd.visited};
+    return launch_dir(L, u);
+  }
+  UBcB<float> u{L.vd.dependences, L.vd.visited};
   return launch_dir(L, u);
 }
 

@@ -96,6 +96,7 @@ struct VData {
   float *old_rank, *new_rank, *contrib;
   double *num_paths;
   float *dependences;
+  double *dep64;  // gg_bc: dependencies accumulated in fp64, stored to dependences at the end
   uint8_t *visited;
   int32_t level, src;
   float damping;

@@ -202,7 +202,10 @@ __device__ __forceinline__ void vertex_udf(int32_t op, int32_t v, const VData &d
       break;
     }
     case GG_VUDF_BC_RESET:  // bc.cpp:28-32, then num_paths[src] = 1, visited[src] = 1
-      d.dependences[v] = 0.0f;
+      if (d.dep64)
+        d.dep64[v] = 0.0;
+      else
+        d.dependences[v] = 0.0f;
       d.num_paths[v] = v == d.src ? 1.0 : 0.0;
       d.visited[v] = v == d.src;
       break;
@@ -214,11 +217,15 @@ __device__ __forceinline__ void vertex_udf(int32_t op, int32_t v, const VData &d
       break;
     case GG_VUDF_BC_BACKWARD_VERTEX:  // bc.cpp:48-51
       d.visited[v] = 1;
-      d.dependences[v] = (float)(d.dependences[v] + 1.0 / d.num_paths[v]);
+      if (d.dep64)
+        d.dep64[v] += 1.0 / d.num_paths[v];
+      else
+        d.dependences[v] = (float)(d.dependences[v] + 1.0 / d.num_paths[v]);
       break;
     case GG_VUDF_BC_FINAL: {  // bc.cpp:56-61
       const double np = d.num_paths[v];
-      d.dependences[v] = np != 0 ? (float)((d.dependences[v] - 1.0 / np) * np) : 0.0f;
+      const double dv = d.dep64 ? d.dep64[v] : (double)d.dependences[v];
+      d.dependences[v] = np != 0 ? (float)((dv - 1.0 / np) * np) : 0.0f;
       break;
     }
     default:

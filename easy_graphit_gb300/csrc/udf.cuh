@@ -89,9 +89,11 @@ struct UBcF {
 };
 
 // bc.cpp:52-54 backward: dependences[dst] += dependences[src] on unvisited dst.
+// T = float is the reference's VertexData<float>; gg_bc accumulates in double.
+template <class T>
 struct UBcB {
   static constexpr bool kWeight = false;
-  float *dep;
+  T *dep;
   const uint8_t *visited;
   __device__ __forceinline__ bool filter(int32_t v) const { return vload(visited + v) == 0; }
   __device__ __forceinline__ bool apply(int32_t s, int32_t d, int32_t) const {
