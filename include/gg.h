@@ -312,6 +312,25 @@ gg_status gg_cc(gg_graph *g, const gg_app_schedule *s, int32_t *labels_out,
 gg_status gg_bc(gg_graph *g, const gg_app_schedule *s, int32_t src,
                 float *dep_out, gg_stats *stats);
 
+/* ----------------------------------------------------- allocation-free BFS
+ * No counterpart in the reference: an extra entry point for callers that may
+ * not allocate device memory while they run (code inside someone else's
+ * pre-sized memory pool or arena, real-time loops that cannot risk an
+ * allocation stall or failure, hosts that keep their allocator to
+ * themselves).  BFS from src over a CSR the caller already holds on the device;
+ * depth_out (device, num_vertices entries) receives the hop distance or -1.
+ * The library allocates nothing here: its scratch is one static device array
+ * sized for at most 1,048,576 vertices (about 8 MiB, held on every GPU that
+ * loads the library until the process exits); larger graphs are rejected with
+ * GG_ERR_INVALID.  The first call on a device looks up that array's address, so
+ * make the first call before capturing the stream into a CUDA graph.  All
+ * calls share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller.  Runs on `stream` (NULL = legacy default stream)
+ * and returns when the result is in depth_out. */
+gg_status gg_bfs_noalloc(const int32_t *offsets, const int32_t *dst,
+                         int32_t num_vertices, int32_t num_edges, int32_t src,
+                         int32_t *depth_out, void *stream);
+
 /* ------------------------------------------------------------ diagnostics
  * Runs a grid barrier that can never complete (it waits for one block more
  * than were launched) with the given time limit, to exercise the bounded-wait
