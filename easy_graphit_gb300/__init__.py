@@ -10,8 +10,10 @@ from .graphit import (  # noqa: F401
     app_schedule,
     bc,
     bfs,
+    bfs_batch,
     cc,
     default_schedule,
     pagerank,
     sssp,
+    sssp_batch,
 )

@@ -115,6 +115,8 @@ SIGNATURES: dict[str, tuple] = {
     "gg_debug_barrier_timeout": (i32, [i32]),
     "gg_kernel_launches": (C.c_uint64, []),
     "gg_bfs_noalloc": (i32, [P, P, i32, i32, i32, P, P]),
+    "gg_bfs_batch": (i32, [P, P, i32, P, C.POINTER(gg_stats)]),
+    "gg_sssp_batch": (i32, [P, P, i32, i32, P, C.POINTER(gg_stats)]),
 }
 
 _lib = None

@@ -1,0 +1,225 @@
+// Batched BFS: up to 64 sources per pass in one persistent kernel.
+//
+// Bit-parallel multi-source BFS: every vertex carries 64-bit masks -- `seen`
+// (sources that reached it), `acc` (sources reaching it this level) and `fr`
+// (sources for which it is on the current frontier).  One traversal of an edge
+// (u, v) serves every source at once: acc[v] |= fr[u] & ~seen[v].  A level ends
+// with a grid barrier, then the vertices touched this level publish their new
+// bits (fr = acc & ~seen, seen |= fr), write depth[s][v] = level for each new
+// bit, and form the next frontier.  Frontier vertices are load-balanced by the
+// TWCE device function of lb.cuh, so hubs are split across a warp or the CTA.
+//
+// The result for each source equals an independent BFS (apps/bfs.cpp), because
+// a source's bit enters seen[v] exactly at the first level that reaches v.
+#include <vector>
+
+#include "engine.h"
+#include "lb.cuh"
+
+namespace gg {
+
+struct MsBfsState {
+  uint64_t *seen, *acc, *fr;  // V each
+  int32_t *qstamp;            // V: last level v was queued at
+  int32_t *q0, *q1;           // V each
+  int32_t *cnt3;              // rotating counts
+  int32_t *depth;             // [nsrc][V] (row-major per source), may be null
+  int64_t depth_stride;       // V
+  int32_t nsrc;
+  uint32_t *bar;
+  int32_t *err;
+  uint64_t timeout_ns;
+  int32_t *stats;             // [0] levels
+  int32_t *stop;
+  uint64_t loop_limit_ns;
+};
+
+// Edge functor for the relax phase.
+struct UMsBfs {
+  static constexpr bool kWeight = false;
+  const uint64_t *seen, *fr;
+  uint64_t *acc;
+  int32_t *qstamp;
+  int32_t level;
+  __device__ __forceinline__ bool src_ok(int32_t) const { return true; }
+  __device__ __forceinline__ bool dst_ok(int32_t) const { return true; }
+  __device__ __forceinline__ int32_t apply(int32_t u, int32_t v, int32_t) const {
+    const uint64_t nb = __ldcg(fr + u) & ~__ldcg(seen + v);
+    if (!nb) return -1;
+    if ((__ldcg(acc + v) & nb) == nb) return -1;  // nothing new for acc
+    atomicOr((unsigned long long *)(acc + v), (unsigned long long)nb);
+    // first toucher this level queues v
+    if (atomicMax(qstamp + v, level) < level) return v;
+    return -1;
+  }
+};
+
+__global__ void __launch_bounds__(512) k_msbfs(DGraph g, MsBfsState st) {
+  extern __shared__ int4 smem[];
+  int32_t *qs[2] = {st.q0, st.q1};
+  int in = 0;
+  int64_t level = 1;
+  const int32_t stride = gridDim.x * blockDim.x;
+  LoopClock clk;
+  clk.start(st.loop_limit_ns);
+  for (;; ++level) {
+    const int32_t n = *(volatile int32_t *)(st.cnt3 + (level - 1) % 3);
+    if (n == 0 || stopped(st.stop, st.err)) break;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st.cnt3[(level + 1) % 3] = 0;
+    // relax: acc[v] |= fr[u] & ~seen[v]
+    {
+      const Enum en{qs[in], nullptr, n};
+      const UMsBfs f{st.seen, st.fr, st.acc, st.qstamp, (int32_t)level};
+      DOut out{};
+      out.mode = OUT_SPARSE;
+      out.q = qs[in ^ 1];
+      out.cnt = st.cnt3 + level % 3;
+      out.cap = g.V;  // qstamp admits each vertex once per level
+      out.err = st.err;
+      const int32_t nv = ceil_div(n, blockDim.x / kStage1);
+      for (int32_t v = blockIdx.x; v < nv; v += gridDim.x)
+        lb_twce<UMsBfs, true>(g, en, n, f, out, v, *reinterpret_cast<TwceSmem *>(smem));
+    }
+    if (!grid_barrier(st.bar, gridDim.x, st.err, st.timeout_ns)) break;
+    // publish: new bits become the next frontier masks
+    {
+      const int32_t m = *(volatile int32_t *)(st.cnt3 + level % 3);
+      const int32_t *q = qs[in ^ 1];
+      for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
+        const int32_t v = q[i];
+        const uint64_t a = __ldcg(st.acc + v);
+        const uint64_t sv = __ldcg(st.seen + v);
+        const uint64_t nb = a & ~sv;
+        st.seen[v] = sv | nb;
+        st.fr[v] = nb;
+        st.acc[v] = 0;
+        if (st.depth) {
+          uint64_t b = nb;
+          while (b) {
+            const int s = __ffsll((long long)b) - 1;
+            b &= b - 1;
+            st.depth[(int64_t)s * st.depth_stride + v] = (int32_t)level;
+          }
+        }
+      }
+    }
+    clk.tick(st.stop);
+    if (!grid_barrier(st.bar, gridDim.x, st.err, st.timeout_ns)) break;
+    in ^= 1;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) st.stats[0] = (int32_t)(level - 1);
+}
+
+// Initial state: masks cleared, depth rows -1, sources seeded.
+__global__ void k_msbfs_init(MsBfsState st, int32_t V, const int32_t *__restrict__ srcs) {
+  const int64_t total = (int64_t)st.nsrc * st.depth_stride;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x)
+    st.depth[i] = -1;
+  for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    st.seen[v] = 0;
+    st.acc[v] = 0;
+    st.fr[v] = 0;
+    st.qstamp[v] = 0;
+  }
+}
+
+__global__ void k_msbfs_seed(MsBfsState st, const int32_t *__restrict__ srcs) {
+  // one thread: sources are few; duplicates share a vertex
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  int32_t n = 0;
+  for (int32_t s = 0; s < st.nsrc; ++s) {
+    const int32_t v = srcs[s];
+    if (!st.seen[v]) st.q0[n++] = v;
+    st.seen[v] |= 1ull << s;
+    st.fr[v] |= 1ull << s;
+    st.depth[(int64_t)s * st.depth_stride + v] = 0;
+  }
+  st.cnt3[0] = n;
+  st.cnt3[1] = 0;
+  st.cnt3[2] = 0;
+  *st.stop = 0;
+}
+
+}  // namespace gg
+
+using namespace gg;
+
+// Batched BFS: depth_out[s*V + v] for nsrc sources (host or device memory).
+extern "C" gg_status gg_bfs_batch(gg_graph *g, const int32_t *sources, int32_t nsrc,
+                                  int32_t *depth_out, gg_stats *stats) {
+  GG_CHECK_ARG(g && sources && nsrc > 0, "bad arguments");
+  const int32_t V = g->csr.V;
+  for (int32_t i = 0; i < nsrc; ++i)
+    GG_CHECK_ARG(sources[i] >= 0 && sources[i] < V, "source out of range");
+  if (stats) *stats = gg_stats{};
+  cudaStream_t st = g->stream;
+  // device arrays (reused across calls through the app slots)
+  uint64_t *masks = nullptr;
+  int32_t *ints = nullptr, *depth = nullptr, *dsrc = nullptr;
+  GG_TRY(scratch_get_app(g, 0, sizeof(uint64_t) * 3 * (size_t)V, (void **)&masks));
+  GG_TRY(scratch_get_app(g, 1, sizeof(int32_t) * (3 * (size_t)V + 64), (void **)&ints));
+  GG_TRY(scratch_get_app(g, 2, sizeof(int32_t) * std::min<int32_t>(nsrc, 64) * (size_t)V, (void **)&depth));
+  GG_TRY(scratch_get_app(g, 3, sizeof(int32_t) * 64, (void **)&dsrc));
+  int per_sm = 0;
+  const int cta = 512;
+  const size_t smem = twce_smem_bytes(cta);
+  GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_msbfs, cta, smem));
+  if (per_sm < 1) return set_error(GG_ERR_UNSUPPORTED, "batched BFS kernel does not fit an SM");
+  const uint64_t l0 = launches();
+  cudaEventRecord(g->ev0, st);
+  float loop_ms = 0;
+  int32_t levels = 0;
+  for (int32_t base = 0; base < nsrc; base += 64) {
+    const int32_t k = std::min(64, nsrc - base);
+    MsBfsState S{};
+    S.seen = masks;
+    S.acc = masks + V;
+    S.fr = masks + 2 * (size_t)V;
+    S.qstamp = ints;
+    S.q0 = ints + V;
+    S.q1 = ints + 2 * (size_t)V;
+    S.cnt3 = ints + 3 * (size_t)V;
+    S.stats = ints + 3 * (size_t)V + 8;
+    S.stop = ints + 3 * (size_t)V + 12;
+    S.loop_limit_ns = loop_timeout_ns();
+    S.depth = depth;
+    S.depth_stride = V;
+    S.nsrc = k;
+    S.bar = g->d_bar;
+    S.err = g->d_err;
+    S.timeout_ns = barrier_timeout_ns();
+    GG_CUDA(cudaMemcpyAsync(dsrc, sources + base, sizeof(int32_t) * k, cudaMemcpyDefault, st));
+    note_launch();
+    k_msbfs_init<<<g->sm_count * 8, 256, 0, st>>>(S, V, dsrc);
+    note_launch();
+    k_msbfs_seed<<<1, 32, 0, st>>>(S, dsrc);
+    GG_CUDA(cudaMemsetAsync(g->d_bar, 0, sizeof(uint32_t) * 2, st));
+    DGraph dg = g->csr.view();
+    dg.nbuckets = 0;
+    void *args[] = {&dg, &S};
+    cudaEventRecord(g->ev2, st);
+    note_launch();
+    GG_CUDA(cudaLaunchCooperativeKernel((const void *)k_msbfs, per_sm * g->sm_count, cta, args, smem, st));
+    cudaEventRecord(g->ev3, st);
+    GG_CUDA(cudaMemcpyAsync(depth_out + (size_t)base * V, depth, sizeof(int32_t) * (size_t)k * V,
+                            cudaMemcpyDefault, st));
+    GG_CUDA(cudaMemcpyAsync(g->h_pinned + 30, S.stats, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    GG_CUDA(cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, g->ev2, g->ev3);
+    loop_ms += ms;
+    levels = std::max(levels, g->h_pinned[30]);
+  }
+  cudaEventRecord(g->ev1, st);
+  GG_CUDA(cudaEventSynchronize(g->ev1));
+  GG_TRY(check_device_error(g, "bfs_batch"));
+  if (stats) {
+    cudaEventElapsedTime(&stats->device_ms, g->ev0, g->ev1);
+    stats->loop_ms = loop_ms;
+    stats->iterations = levels;
+    stats->fused = 1;
+    stats->launches = (int32_t)(launches() - l0);
+  }
+  return GG_OK;
+}

@@ -193,6 +193,24 @@ __device__ __forceinline__ bool grid_barrier(uint32_t *bar, uint32_t nblocks, in
   return ok_s != 0;
 }
 
+// Wall-clock bound of a persistent loop.  Block 0 raises *stop just before an
+// iteration's closing grid barrier, so every block reads the same value at the
+// top of the next iteration and all leave together (DEV_ERR_TIMEOUT recorded).
+struct LoopClock {
+  uint64_t deadline;
+  __device__ __forceinline__ void start(uint64_t limit_ns) { deadline = globaltimer_ns() + limit_ns; }
+  __device__ __forceinline__ void tick(int32_t *stop) const {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && globaltimer_ns() > deadline) atomicExch(stop, 1);
+  }
+};
+__device__ __forceinline__ bool stopped(const int32_t *stop, int32_t *err) {
+  if (*(volatile const int32_t *)stop) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, DEV_ERR_TIMEOUT);
+    return true;
+  }
+  return false;
+}
+
 __host__ __device__ __forceinline__ int32_t ceil_div(int64_t a, int64_t b) {
   return (int32_t)((a + b - 1) / b);
 }

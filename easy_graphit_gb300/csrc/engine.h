@@ -169,5 +169,6 @@ gg_status fused_bfs(gg_graph *g, const gg_schedule *s, int32_t src, const VData 
 gg_status fused_sssp(gg_graph *g, const gg_schedule *s, int32_t src, int32_t delta, const VData &vd,
                      gg_frontier *f, int32_t *iters, int64_t *advances, bool *ran);
 uint64_t barrier_timeout_ns();
+uint64_t loop_timeout_ns();  // wall-clock bound of one persistent loop (GG_LOOP_TIMEOUT_MS)
 
 }  // namespace gg

@@ -24,6 +24,15 @@ uint64_t barrier_timeout_ns() {
   return t;
 }
 
+uint64_t loop_timeout_ns() {
+  static uint64_t t = [] {
+    const char *e = getenv("GG_LOOP_TIMEOUT_MS");
+    const long ms = e ? atol(e) : 0;
+    return (uint64_t)(ms > 0 ? ms : 120000) * 1000000ull;
+  }();
+  return t;
+}
+
 bool fused_supported(const gg_schedule *s) {
   if (s->direction != GG_PUSH || s->frontier_creation != GG_FC_SPARSE) return false;
   switch (s->load_balancing) {
@@ -69,6 +78,8 @@ struct FusedArgs {
   VData vd;
   int32_t delta;
   int32_t *gmin2;  // SSSP bucket-advance minima [2]
+  int32_t *stop;   // loop time limit flag (see LoopClock)
+  uint64_t loop_limit_ns;
 };
 
 __device__ __forceinline__ DOut sparse_out(const FusedArgs &a, int32_t *q, int64_t it) {
@@ -87,14 +98,17 @@ __global__ void __launch_bounds__(1024) k_bfs_fused(FusedArgs a) {
   int32_t *qs[2] = {a.q0, a.q1};
   int in = 0;
   int64_t level = 1;
+  LoopClock clk;
+  clk.start(a.loop_limit_ns);
   for (;; ++level) {
     const int32_t n = *(volatile int32_t *)(a.cnt3 + (level - 1) % 3);
-    if (n == 0 || *(volatile int32_t *)a.err) break;
+    if (n == 0 || stopped(a.stop, a.err)) break;
     if (blockIdx.x == 0 && threadIdx.x == 0) a.cnt3[(level + 1) % 3] = 0;
     const Enum en{qs[in], nullptr, n};
     const EdgeF<UBfs, false> f{UBfs{a.vd.parent, a.vd.depth, (int32_t)level},
                                DIn{IN_ALL, nullptr, nullptr}, DIn{IN_ALL, nullptr, nullptr}, true};
     run_lb<LB>(a.g, en, n, f, sparse_out(a, qs[in ^ 1], level), smem);
+    clk.tick(a.stop);
     if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
     in ^= 1;
   }
@@ -112,9 +126,11 @@ __global__ void __launch_bounds__(1024) k_sssp_fused(FusedArgs a) {
   const int32_t V = a.g.V;
   int in = 0;
   int64_t it = 1, cur = 0, adv = 0, relax = 0;
+  LoopClock clk;
+  clk.start(a.loop_limit_ns);
   for (;; ++it) {
     const int32_t n = *(volatile int32_t *)(a.cnt3 + (it - 1) % 3);
-    if (*(volatile int32_t *)a.err) break;
+    if (stopped(a.stop, a.err)) break;
     if (blockIdx.x == 0 && threadIdx.x == 0) a.cnt3[(it + 1) % 3] = 0;
     if (n == 0) {
       const int64_t window = cur + a.delta;
@@ -168,6 +184,7 @@ __global__ void __launch_bounds__(1024) k_sssp_fused(FusedArgs a) {
       run_lb<LB>(a.g, en, n, f, sparse_out(a, qs[in ^ 1], it), smem);
       ++relax;
     }
+    clk.tick(a.stop);
     if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
     in ^= 1;
   }
@@ -215,6 +232,8 @@ static FusedArgs make_args(gg_graph *g, gg_frontier *f, const VData &vd) {
   a.stats = g->d_misc + 44;
   a.vd = vd;
   a.gmin2 = g->d_misc + 46;
+  a.stop = g->d_misc + 48;
+  a.loop_limit_ns = loop_timeout_ns();
   return a;
 }
 
@@ -229,7 +248,8 @@ static gg_status init_counts(gg_graph *g) {
   h[5] = 0;
   h[6] = INT_MAX;
   h[7] = INT_MAX;
-  GG_CUDA(cudaMemcpyAsync(g->d_misc + 40, h, sizeof(int32_t) * 8, cudaMemcpyHostToDevice, g->stream));
+  h[8] = 0;  // stop flag
+  GG_CUDA(cudaMemcpyAsync(g->d_misc + 40, h, sizeof(int32_t) * 9, cudaMemcpyHostToDevice, g->stream));
   return GG_OK;
 }
 

@@ -459,6 +459,29 @@ def cc(g: GraphT, schedule=None):
     return labels, _stats(st)
 
 
+def bfs_batch(g: GraphT, sources, out=None):
+    """Batched BFS from many sources in one persistent launch per 64 sources.
+    Returns (depth [nsrc, V] int32, stats); `out` may be a preallocated
+    numpy array or CUDA tensor of that shape."""
+    srcs = np.ascontiguousarray(sources, dtype=np.int32)
+    if out is None:
+        out = np.empty((len(srcs), g.num_vertices), dtype=np.int32)
+    st = L.gg_stats()
+    call("gg_bfs_batch", g.handle, _np_ptr(srcs), len(srcs), _ptr(out), C.byref(st))
+    return out, _stats(st)
+
+
+def sssp_batch(g: GraphT, sources, delta: int, out=None):
+    """Batched delta-stepping SSSP (32 sources per pass).  Returns
+    (dist [nsrc, V] int32, stats)."""
+    srcs = np.ascontiguousarray(sources, dtype=np.int32)
+    if out is None:
+        out = np.empty((len(srcs), g.num_vertices), dtype=np.int32)
+    st = L.gg_stats()
+    call("gg_sssp_batch", g.handle, _np_ptr(srcs), len(srcs), delta, _ptr(out), C.byref(st))
+    return out, _stats(st)
+
+
 def bc(g: GraphT, src: int, schedule=None, fuse=None):
     """apps/bc.cpp: returns (dependences fp32, stats)."""
     dep = np.empty(g.num_vertices, dtype=np.float32)

@@ -331,6 +331,20 @@ gg_status gg_bfs_noalloc(const int32_t *offsets, const int32_t *dst,
                          int32_t num_vertices, int32_t num_edges, int32_t src,
                          int32_t *depth_out, void *stream);
 
+/* ------------------------------------------------------------ batched mode
+ * Many sources in one persistent launch (no reference counterpart: the
+ * reference runs one source per testcase() trial).  Results equal nsrc
+ * independent runs of gg_bfs / gg_sssp.
+ *  gg_bfs_batch: bit-parallel multi-source BFS, 64 sources per pass;
+ *    depth_out[s*V + v] (host or device memory, nsrc*V int32).
+ *  gg_sssp_batch: 32 sources per pass with per-source delta-stepping windows
+ *    (gpu_priority_queue.h semantics) and a far pile instead of O(V) bucket
+ *    scans; dist_out[s*V + v] (INT_MAX unreached). */
+gg_status gg_bfs_batch(gg_graph *g, const int32_t *sources, int32_t nsrc,
+                       int32_t *depth_out, gg_stats *stats);
+gg_status gg_sssp_batch(gg_graph *g, const int32_t *sources, int32_t nsrc,
+                        int32_t delta, int32_t *dist_out, gg_stats *stats);
+
 /* ------------------------------------------------------------ diagnostics
  * Runs a grid barrier that can never complete (it waits for one block more
  * than were launched) with the given time limit, to exercise the bounded-wait
