@@ -4,8 +4,11 @@
 Workload (default, one GPU): SSSP delta-stepping on a directed R-MAT graph of
 scale 22, edge factor 16 (a/b/c = 0.57/0.19/0.19, GAPBS seed 27491095), int32
 weights U[1,255]; 32 sources from GAPBS's SourcePicker; one step = SSSP from all
-32 sources.  Inputs are synthetic (the reference's datasets are not available).
-TEPS counts each reached vertex's out-edges once per source (E_r).
+32 sources in the batched mode (one persistent launch).  Delta is 32 (from the
+configured sweep {1,8,32,128}; --delta 0 autotunes over it).  The plain path -- the reference's default
+schedule, one source at a time -- is measured beside it.  Inputs are synthetic
+(the reference's datasets are not available).  TEPS counts each reached
+vertex's out-edges once per source (E_r).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
   torchrun ... bench.py --gpus N     (one rank per GPU; sources shard by rank)
@@ -45,7 +48,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     p.add_argument("--scale", type=int, default=SCALE)
-    p.add_argument("--delta", type=int, default=0, help="0 = pick by a short autotune")
+    p.add_argument("--delta", type=int, default=32,
+                   help="delta-stepping bucket width (both arms); 0 = autotune over {1,8,32,128}")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
@@ -152,7 +156,7 @@ def peaks():
 
 def ncu_traffic():
     """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
-    f = ROOT / "profiles" / "sssp_fused_vertex_rmat22.md"
+    f = ROOT / "profiles" / "sssp_batch_rmat22.md"
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
@@ -197,12 +201,13 @@ def run_reference(args):
 
 
 def run_gb300(args):
+    import ctypes as C
+
     import torch
     import torch.distributed as dist
 
     from easy_graphit_gb300 import GraphT, _lib as L, app_schedule, default_schedule
-    from easy_graphit_gb300.graphit import _ptr
-    import ctypes as C
+    from easy_graphit_gb300 import SimpleGPUSchedule as T
 
     rank, world, local = dist_env()
     if world > 1:
@@ -215,61 +220,74 @@ def run_gb300(args):
     V, E = hg.num_vertices, hg.num_edges
     # weak scaling: every rank traverses its own 32 sources on its own replica
     sources = hg.pick_sources(N_SOURCES, seed=27491095 + rank)
+    h_src = np.ascontiguousarray(sources, dtype=np.int32)
 
     g = GraphT(hg)
     stream = torch.cuda.current_stream(dev)
     g.set_stream(stream.cuda_stream)
-    sch, fuse = default_schedule("sssp")  # PUSH, SPARSE, VERTEX_BASED, fused (sssp.cpp:76-79)
-    a = app_schedule(sch, fuse)
     dist_dev = torch.empty((N_SOURCES, V), dtype=torch.int32, device=dev)
+    base = dist_dev.data_ptr()
     st = L.gg_stats()
 
-    def one(src, out_ptr, stats=True):
-        L.call("gg_sssp", g.handle, C.byref(a), int(src), delta, out_ptr,
-               C.byref(st) if stats else None)
+    def batched(delta_, out_ptr, stats=True):
+        L.call("gg_sssp_batch", g.handle, C.c_void_p(h_src.ctypes.data), N_SOURCES, delta_,
+               C.c_void_p(out_ptr), C.byref(st) if stats else None)
         return st.loop_ms
 
-    # Delta: all four give identical distances; pick the fastest on one source.
+    # Delta from the configured sweep, picked by a short autotune (all four
+    # give identical distances).
     delta = args.delta
     if not delta:
         best = None
         for d in DELTAS:
-            delta = d
-            one(sources[0], C.c_void_p(dist_dev[0].data_ptr()))
-            t = one(sources[0], C.c_void_p(dist_dev[0].data_ptr()))
+            batched(d, base)
+            t = min(batched(d, base) for _ in range(2))
             if best is None or t < best[0]:
                 best = (t, d)
         delta = best[1]
 
-    # Algorithmic work per source (untimed pass): E_r, V_r.
-    er, vr, loop_ms = [], [], []
-    for i, s in enumerate(sources):
-        one(s, C.c_void_p(dist_dev[i].data_ptr()))
-        d = dist_dev[i].cpu().numpy()
-        v_r, e_r = reached_stats(off, d)
+    # Algorithmic work per source (untimed): E_r, V_r from the distances.
+    batched(delta, base)
+    dd = dist_dev.cpu().numpy()
+    er, vr = [], []
+    for i in range(N_SOURCES):
+        v_r, e_r = reached_stats(off, dd[i])
         er.append(e_r)
         vr.append(v_r)
     total_edges = float(sum(er))
 
-    def step(out_base, stride_bytes):
+    # Plain path for comparison (untimed for `value`): the reference's default
+    # SSSP schedule (PUSH, SPARSE, VERTEX_BASED, fused; sssp.cpp:76-79), one
+    # source at a time; and the single-source TWCE fused schedule.
+    def single(sch_, fuse_):
+        a_ = app_schedule(sch_, fuse_)
+        t_ = 0.0
         for i, s in enumerate(sources):
-            one(s, C.c_void_p(out_base + i * stride_bytes))
+            L.call("gg_sssp", g.handle, C.byref(a_), int(s), delta, C.c_void_p(base + i * V * 4),
+                   C.byref(st))
+            t_ += st.device_ms
+        return total_edges / (t_ / 1e3) / 1e9
+    plain_sch, plain_fuse = default_schedule("sssp")
+    plain_gteps = single(plain_sch, plain_fuse)
+    twce = T()
+    twce.configLoadBalancing(T.load_balancing_type.TWCE)
+    twce_gteps = single(twce, True)
+    batched(delta, base)
+    assert np.array_equal(dist_dev.cpu().numpy(), dd), "batched and single-source distances differ"
 
-    base = dist_dev.data_ptr()
     for _ in range(args.warmup):
-        step(base, V * 4)
+        batched(delta, base)
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
     l0 = L.lib().gg_kernel_launches()
+    loop_ms = []
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         ev0.record(stream)
         for _ in range(args.steps):
-            for i, s in enumerate(sources):
-                one(s, C.c_void_p(base + i * V * 4))
-                loop_ms.append(st.loop_ms)
+            loop_ms.append(batched(delta, base))
         ev1.record(stream)
         torch.cuda.synchronize()
     launches = int(L.lib().gg_kernel_launches() - l0)
@@ -282,12 +300,12 @@ def run_gb300(args):
     value = total_edges * world / (ms_per_step / 1e3) / 1e9
 
     # End to end through the C ABI with host buffers: upload the CSR from
-    # pinned host memory, run the 32 sources with distances written to pinned
-    # host memory, release the graph -- all inside the timed region.
+    # pinned host memory, run the batch with distances written to pinned host
+    # memory, release the graph -- all inside the timed region.
     pin = lambda a_: torch.from_numpy(a_).pin_memory()
     h_off, h_dst, h_w = pin(off), pin(dst), pin(w)
     h_out = torch.empty((N_SOURCES, V), dtype=torch.int32).pin_memory()
-    h2d = (off.nbytes + dst.nbytes + w.nbytes)
+    h2d = off.nbytes + dst.nbytes + w.nbytes + h_src.nbytes
     d2h = N_SOURCES * V * 4
     e2e_steps = max(1, min(args.steps, 3))
     torch.cuda.synchronize()
@@ -295,13 +313,12 @@ def run_gb300(args):
     for _ in range(e2e_steps):
         ge = GraphT(offsets=h_off, dst=h_dst, weights=h_w)
         ge.set_stream(stream.cuda_stream)
-        for i, s in enumerate(sources):
-            L.call("gg_sssp", ge.handle, C.byref(a), int(s), delta,
-                   C.c_void_p(h_out.data_ptr() + i * V * 4), None)
+        L.call("gg_sssp_batch", ge.handle, C.c_void_p(h_src.ctypes.data), N_SOURCES, delta,
+               C.c_void_p(h_out.data_ptr()), None)
         ge.close()
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
-    assert np.array_equal(h_out[0].numpy(), dist_dev[0].cpu().numpy())
+    assert np.array_equal(h_out.numpy(), dd)
     e2e_val = total_edges * world / (e2e_ms / 1e3) / 1e9
 
     if rank != 0:
@@ -309,9 +326,8 @@ def run_gb300(args):
             dist.destroy_process_group()
         return
     peak, peak_kind = peaks()
-    alg_bytes = [12.0 * e + 16.0 * v for e, v in zip(er, vr)]
-    lm = np.array(loop_ms).reshape(args.steps, N_SOURCES).mean(axis=0)  # per source
-    achieved = float(np.sum(alg_bytes) / (np.sum(lm) / 1e3) / 1e9)
+    alg_bytes = float(sum(12.0 * e + 16.0 * v for e, v in zip(er, vr)))
+    achieved = alg_bytes / (float(np.mean(loop_ms)) / 1e3) / 1e9
     traffic = ncu_traffic()
     cpu = None
     if not args.no_cpu_baseline:
@@ -325,15 +341,19 @@ def run_gb300(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
         "config": {"workload": f"sssp_delta_stepping_rmat{args.scale}_k16_directed",
                    "V": V, "E": E, "sources": N_SOURCES, "delta": delta,
-                   "weights": "U[1,255]", "schedule": "PUSH SPARSE VERTEX_BASED fused (sssp.cpp default)",
-                   "mode": "plain single-source", "l2": "inputs larger than L2 (CSR %.2f GB)"
-                   % ((off.nbytes + dst.nbytes + w.nbytes) / 1e9),
+                   "delta_sweep": list(DELTAS), "weights": "U[1,255]",
+                   "mode": "batched: 32 sources per persistent launch (gg_sssp_batch)",
+                   "plain_gteps": plain_gteps,
+                   "plain_schedule": "PUSH SPARSE VERTEX_BASED fused, one source at a time (sssp.cpp default)",
+                   "single_twce_gteps": twce_gteps,
+                   "batched_over_plain": value / world / plain_gteps,
+                   "l2": "inputs larger than L2 (CSR %.2f GB, distances %.2f GB)"
+                   % ((off.nbytes + dst.nbytes + w.nbytes) / 1e9, N_SOURCES * V * 4 / 1e9),
                    "parallelism": f"replicas x{world}, sources by rank"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "k_sssp_fused<VERTEX_BASED>",
-                     "peak_kind": peak_kind,
-                     "bytes_model": "12*E_r + 16*V_r per source"},
+                     "kernel": "k_bsssp", "peak_kind": peak_kind,
+                     "bytes_model": "sum over sources of 12*E_r + 16*V_r per launch"},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_val, "unit": "GTEPS", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
