@@ -27,6 +27,10 @@ namespace gg {
 
 constexpr int32_t kChunk = 256;  // edges per queue entry
 constexpr int32_t kLanes = 32;
+constexpr int32_t kPrefetch = 8;  // distance lines in flight per warp
+// Queue entries active for at most this many sources are relaxed edge-parallel
+// (lanes = edges); busier ones source-parallel (lanes = sources).
+constexpr int32_t kEdgeParallelMax = 6;
 
 struct BsState {
   int32_t *dist;            // [V][32]
@@ -99,6 +103,35 @@ __global__ void __launch_bounds__(256) k_bsssp(BsState S) {
         const int32_t du = act ? __ldcg(S.dist + (int64_t)u * kLanes + lane) : INT_MAX;
         const int32_t b = S.off[u] + c * kChunk;
         const int32_t eend = min(b + kChunk, S.off[u + 1]);
+        if (__popc(m) <= kEdgeParallelMax) {
+          // Few active sources: lanes take edges, the warp loops over sources.
+          uint32_t mm = m;
+          while (mm) {
+            const int32_t s = __ffs(mm) - 1;
+            mm &= mm - 1;
+            const int32_t du_s = __shfl_sync(0xffffffffu, du, s);
+            const int32_t cut_s = __shfl_sync(0xffffffffu, cut, s);
+            if (du_s == INT_MAX) continue;
+            for (int32_t k = b + lane; k < eend; k += 32) {
+              const int32_t v = __ldg(S.dst + k);
+              const int32_t np = du_s + __ldg(S.w + k);
+              int32_t *pd = S.dist + (int64_t)v * kLanes + s;
+              if (np < __ldcg(pd) && atomicMin(pd, np) > np) {
+                if (np < cut_s) {
+                  atomicOr(S.nacc + v, 1u << s);
+                  if (atomicMax(S.qstamp + v, it) < it) bs_enqueue(S, qo, qcnt_out, v);
+                } else if (atomicOr(S.far + v, 1u << s) == 0u) {
+                  const int32_t pos = atomicAdd(S.cnt + 3 + p, 1);
+                  if (pos < S.V)
+                    S.fl[p][pos] = v;
+                  else
+                    atomicOr(S.err, DEV_ERR_OVERFLOW);
+                }
+              }
+            }
+          }
+          continue;
+        }
         for (int32_t k0 = b; k0 < eend; k0 += 32) {
           int32_t vv = 0, ww = 0;
           if (k0 + lane < eend) {
@@ -106,31 +139,43 @@ __global__ void __launch_bounds__(256) k_bsssp(BsState S) {
             ww = __ldg(S.w + k0 + lane);
           }
           const int32_t cnt = min(32, eend - k0);
-          for (int32_t j = 0; j < cnt; ++j) {
-            const int32_t v = __shfl_sync(0xffffffffu, vv, j);
-            const int32_t wt = __shfl_sync(0xffffffffu, ww, j);
-            bool near = false, farb = false;
-            if (act && du != INT_MAX) {
-              const int32_t np = du + wt;
-              int32_t *pd = S.dist + (int64_t)v * kLanes + lane;
-              if (np < __ldcg(pd) && atomicMin(pd, np) > np) {
-                near = np < cut;
-                farb = !near;
-              }
+          const bool live = act && du != INT_MAX;
+          for (int32_t j0 = 0; j0 < cnt; j0 += kPrefetch) {
+            // Issue the distance-line loads of kPrefetch edges before using
+            // them.  A stale (larger) value only costs an extra atomicMin.
+            int32_t vs[kPrefetch], ws[kPrefetch], dvs[kPrefetch];
+#pragma unroll
+            for (int32_t t = 0; t < kPrefetch; ++t) {
+              vs[t] = __shfl_sync(0xffffffffu, vv, (j0 + t) & 31);
+              ws[t] = __shfl_sync(0xffffffffu, ww, (j0 + t) & 31);
+              dvs[t] = (live && j0 + t < cnt) ? __ldcg(S.dist + (int64_t)vs[t] * kLanes + lane) : INT_MIN;
             }
-            const uint32_t nb = __ballot_sync(0xffffffffu, near);
-            const uint32_t fb = __ballot_sync(0xffffffffu, farb);
-            if (lane == 0) {
-              if (nb) {
-                atomicOr(S.nacc + v, nb);
-                if (atomicMax(S.qstamp + v, it) < it) bs_enqueue(S, qo, qcnt_out, v);
+#pragma unroll
+            for (int32_t t = 0; t < kPrefetch; ++t) {
+              if (j0 + t >= cnt) break;  // warp-uniform
+              const int32_t v = vs[t];
+              bool near = false, farb = false;
+              if (live) {
+                const int32_t np = du + ws[t];
+                if (np < dvs[t] && atomicMin(S.dist + (int64_t)v * kLanes + lane, np) > np) {
+                  near = np < cut;
+                  farb = !near;
+                }
               }
-              if (fb && atomicOr(S.far + v, fb) == 0u) {
-                const int32_t pos = atomicAdd(S.cnt + 3 + p, 1);
-                if (pos < S.V)
-                  S.fl[p][pos] = v;
-                else
-                  atomicOr(S.err, DEV_ERR_OVERFLOW);
+              const uint32_t nb = __ballot_sync(0xffffffffu, near);
+              const uint32_t fb = __ballot_sync(0xffffffffu, farb);
+              if (lane == 0) {
+                if (nb) {
+                  atomicOr(S.nacc + v, nb);
+                  if (atomicMax(S.qstamp + v, it) < it) bs_enqueue(S, qo, qcnt_out, v);
+                }
+                if (fb && atomicOr(S.far + v, fb) == 0u) {
+                  const int32_t pos = atomicAdd(S.cnt + 3 + p, 1);
+                  if (pos < S.V)
+                    S.fl[p][pos] = v;
+                  else
+                    atomicOr(S.err, DEV_ERR_OVERFLOW);
+                }
               }
             }
           }
