@@ -2,6 +2,7 @@
 vertexset.apply frontier operators and the BFS, SSSP, PageRank, CC and BC apps)
 as hand-written sm_103a CUDA behind a C ABI (libgg.so, include/gg.h)."""
 from .graphit import (  # noqa: F401
+    BatchPlan,
     GraphT,
     HostGraph,
     HybridGPUSchedule,
@@ -11,9 +12,12 @@ from .graphit import (  # noqa: F401
     bc,
     bfs,
     bfs_batch,
+    bfs_multi,
     cc,
     default_schedule,
+    multigraph_batch,
     pagerank,
     sssp,
     sssp_batch,
+    sssp_multi,
 )

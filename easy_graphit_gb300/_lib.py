@@ -116,6 +116,12 @@ SIGNATURES: dict[str, tuple] = {
     "gg_kernel_launches": (C.c_uint64, []),
     "gg_bfs_noalloc": (i32, [P, P, i32, i32, i32, P, P]),
     "gg_bfs_batch": (i32, [P, P, i32, P, C.POINTER(gg_stats)]),
+    "gg_bfs_multi": (i32, [P, C.POINTER(gg_app_schedule), P, i32, P, P, C.POINTER(gg_stats)]),
+    "gg_sssp_multi": (i32, [P, C.POINTER(gg_app_schedule), P, i32, i32, P, C.POINTER(gg_stats)]),
+    "gg_host_graph_union": (i32, [P, i32, P, C.POINTER(P)]),
+    "gg_batch_plan_create": (i32, [P, i32, P, i32, i32, P, C.POINTER(P)]),
+    "gg_batch_plan_run": (i32, [P, C.POINTER(gg_stats)]),
+    "gg_batch_plan_destroy": (i32, [P]),
     "gg_sssp_batch": (i32, [P, P, i32, i32, P, C.POINTER(gg_stats)]),
 }
 

@@ -146,21 +146,57 @@ gg_status scratch_get_app(gg_graph *g, int slot, size_t bytes, void **p) {
   return GG_OK;
 }
 
-gg_status run_bfs(gg_graph *g, const gg_app_schedule *s, int32_t src, int32_t *parent,
-                  int32_t *depth, gg_stats *st) {
+// Multi-source start: parent[s] = s, depth[s] = 0 (BFS) or dist[s] = 0 (SSSP)
+// for every source, and the frontier queue holds the sources.
+__global__ void k_seed_sources(int32_t sssp, VData d, const int32_t *__restrict__ srcs, int32_t n,
+                               int32_t *__restrict__ q, int32_t *__restrict__ cnt) {
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int32_t s = srcs[i];
+    if (sssp) {
+      d.dist[s] = 0;
+    } else {
+      d.parent[s] = s;
+      if (d.depth) d.depth[s] = 0;
+    }
+    q[i] = s;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *cnt = n;
+}
+
+gg_status seed_sources(gg_graph *g, gg_frontier *f, bool sssp, const VData &vd, const int32_t *srcs,
+                       int32_t n) {
+  int32_t *dsrc = nullptr;
+  GG_TRY(scratch_get(g, 0, sizeof(int32_t) * ((size_t)std::max(n, 1) + (size_t)g->csr.V + 32),
+                     (void **)&dsrc));
+  GG_CUDA(cudaMemcpyAsync(dsrc, srcs, sizeof(int32_t) * n, cudaMemcpyDefault, g->stream));
+  GG_CUDA(cudaMemsetAsync(f->cnt, 0, sizeof(int32_t) * 2, g->stream));
+  note_launch();
+  k_seed_sources<<<std::max(1, std::min(ceil_div(n, 256), 1024)), 256, 0, g->stream>>>(
+      sssp, vd, dsrc, n, f->q_in, f->cnt_in);
+  GG_CUDA(cudaGetLastError());
+  f->fmt = GG_FMT_SPARSE;
+  GG_CUDA(cudaStreamSynchronize(g->stream));  // dsrc is reused by the next scratch user
+  return GG_OK;
+}
+
+gg_status run_bfs(gg_graph *g, const gg_app_schedule *s, const int32_t *srcs, int32_t nsrc,
+                  int32_t *parent, int32_t *depth, gg_stats *st) {
   const int32_t V = g->csr.V;
   gg_frontier *f = nullptr;
   GG_TRY(app_frontier(g, &f));
   VData vd{};
   vd.parent = parent;
   vd.depth = depth;
-  vd.src = src;
+  vd.src = nsrc == 1 ? srcs[0] : -1;
   GG_TRY(vertexset_apply_impl(g, nullptr, GG_VUDF_BFS_RESET, vd));  // reset + parent[src]=src
-  GG_TRY(frontier_set_single(f, src));
+  if (nsrc == 1)
+    GG_TRY(frontier_set_single(f, srcs[0]));
+  else
+    GG_TRY(seed_sources(g, f, false, vd, srcs, nsrc));
   if (s->fuse && s->kind == GG_SCHED_SIMPLE && fused_supported(&s->s1)) {
     bool ran = false;
     int32_t iters = 0;
-    GG_TRY(fused_bfs(g, &s->s1, src, vd, f, &iters, &ran));
+    GG_TRY(fused_bfs(g, &s->s1, nsrc, vd, f, &iters, &ran));
     if (ran) {
       if (st) {
         st->iterations = iters;
@@ -185,8 +221,9 @@ gg_status run_bfs(gg_graph *g, const gg_app_schedule *s, int32_t src, int32_t *p
   return check_device_error(g, "bfs");
 }
 
-gg_status run_sssp(gg_graph *g, const gg_app_schedule *s, int32_t src, int32_t delta, int32_t *dist,
-                   gg_stats *st) {
+gg_status run_sssp(gg_graph *g, const gg_app_schedule *s, const int32_t *srcs, int32_t nsrc,
+                   int32_t delta, int32_t *dist, gg_stats *st) {
+  const int32_t src = nsrc == 1 ? srcs[0] : -1;
   if (!g->app_pq) {
     GG_TRY(gg_pq_create(g, dist, 0, delta, src, &g->app_pq));
   }
@@ -197,11 +234,12 @@ gg_status run_sssp(gg_graph *g, const gg_app_schedule *s, int32_t src, int32_t d
   vd.dist = dist;
   vd.src = src;
   GG_TRY(vertexset_apply_impl(g, nullptr, GG_VUDF_SSSP_RESET, vd));  // reset + SP[src]=0
+  if (nsrc > 1) GG_TRY(seed_sources(g, pq->frontier, true, vd, srcs, nsrc));
   if (s->fuse && s->kind == GG_SCHED_SIMPLE && fused_supported(&s->s1)) {
     bool ran = false;
     int32_t iters = 0;
     int64_t adv = 0;
-    GG_TRY(fused_sssp(g, &s->s1, src, delta, vd, pq->frontier, &iters, &adv, &ran));
+    GG_TRY(fused_sssp(g, &s->s1, nsrc, delta, vd, pq->frontier, &iters, &adv, &ran));
     if (ran) {
       if (st) {
         st->iterations = iters;
@@ -247,7 +285,7 @@ gg_status gg_bfs(gg_graph *g, const gg_app_schedule *s, int32_t src, int32_t *de
   GG_TRY(app_array(g, 0, V, &parent));
   GG_TRY(app_array(g, 1, V, &depth));
   Trial t(g);
-  GG_TRY(run_bfs(g, s, src, parent, depth, st));
+  GG_TRY(run_bfs(g, s, &src, 1, parent, depth, st));
   GG_TRY(t.stop(st));
   if (depth_out) GG_CUDA(cudaMemcpyAsync(depth_out, depth, sizeof(int32_t) * V, cudaMemcpyDefault, g->stream));
   if (parent_out) GG_CUDA(cudaMemcpyAsync(parent_out, parent, sizeof(int32_t) * V, cudaMemcpyDefault, g->stream));
@@ -266,7 +304,50 @@ gg_status gg_sssp(gg_graph *g, const gg_app_schedule *s, int32_t src, int32_t de
   int32_t *dist = nullptr;
   GG_TRY(app_array(g, 2, V, &dist));
   Trial t(g);
-  GG_TRY(run_sssp(g, s, src, delta, dist, st));
+  GG_TRY(run_sssp(g, s, &src, 1, delta, dist, st));
+  GG_TRY(t.stop(st));
+  if (dist_out) GG_CUDA(cudaMemcpyAsync(dist_out, dist, sizeof(int32_t) * V, cudaMemcpyDefault, g->stream));
+  GG_TRY(reach_stats(g, dist, st));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  return GG_OK;
+}
+
+// Multi-source traversals: every source starts at depth / distance 0 and the
+// result is the distance to the nearest source.  On a disjoint union of graphs
+// with one source per graph (gg_host_graph_union) this is each graph's own
+// BFS / SSSP, computed for all graphs in one traversal.
+gg_status gg_bfs_multi(gg_graph *g, const gg_app_schedule *s, const int32_t *sources, int32_t n,
+                       int32_t *depth_out, int32_t *parent_out, gg_stats *st) {
+  GG_TRY(check_app(g, s));
+  GG_CHECK_ARG(sources && n >= 1, "need at least one source");
+  const int32_t V = g->csr.V;
+  for (int32_t i = 0; i < n; ++i) GG_CHECK_ARG(sources[i] >= 0 && sources[i] < V, "source out of range");
+  if (st) *st = gg_stats{};
+  int32_t *parent = nullptr, *depth = nullptr;
+  GG_TRY(app_array(g, 0, V, &parent));
+  GG_TRY(app_array(g, 1, V, &depth));
+  Trial t(g);
+  GG_TRY(run_bfs(g, s, sources, n, parent, depth, st));
+  GG_TRY(t.stop(st));
+  if (depth_out) GG_CUDA(cudaMemcpyAsync(depth_out, depth, sizeof(int32_t) * V, cudaMemcpyDefault, g->stream));
+  if (parent_out) GG_CUDA(cudaMemcpyAsync(parent_out, parent, sizeof(int32_t) * V, cudaMemcpyDefault, g->stream));
+  GG_TRY(reach_stats(g, depth, st));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  return GG_OK;
+}
+
+gg_status gg_sssp_multi(gg_graph *g, const gg_app_schedule *s, const int32_t *sources, int32_t n,
+                        int32_t delta, int32_t *dist_out, gg_stats *st) {
+  GG_TRY(check_app(g, s));
+  GG_CHECK_ARG(sources && n >= 1, "need at least one source");
+  GG_CHECK_ARG(delta >= 1, "delta must be >= 1");
+  const int32_t V = g->csr.V;
+  for (int32_t i = 0; i < n; ++i) GG_CHECK_ARG(sources[i] >= 0 && sources[i] < V, "source out of range");
+  if (st) *st = gg_stats{};
+  int32_t *dist = nullptr;
+  GG_TRY(app_array(g, 2, V, &dist));
+  Trial t(g);
+  GG_TRY(run_sssp(g, s, sources, n, delta, dist, st));
   GG_TRY(t.stop(st));
   if (dist_out) GG_CUDA(cudaMemcpyAsync(dist_out, dist, sizeof(int32_t) * V, cudaMemcpyDefault, g->stream));
   GG_TRY(reach_stats(g, dist, st));

@@ -1,0 +1,77 @@
+// Shared declarations of the batched mode (batch_bfs.cu, batch_sssp.cu) and its
+// CUDA-graph plans (batch_plan.cu).
+#pragma once
+
+#include "engine.h"
+
+namespace gg {
+
+constexpr int32_t kBsLanes = 32;  // sources per batched-SSSP pass (warp lanes)
+constexpr int32_t kMsBfsWidth = 64;  // sources per batched-BFS pass (mask bits)
+
+// ---------------------------------------------------------- batched SSSP
+struct BsState {
+  int32_t *dist;              // [V][32]
+  uint32_t *fr, *nacc, *far;  // [V] masks
+  int32_t *qstamp;            // [V]
+  int64_t *q[2];              // queue entries (u << 32 | chunk)
+  int64_t qcap;
+  int32_t *fl[2];             // far lists
+  int32_t *cnt;               // [0..2] queue counts (rotating), [3..4] far counts, [5..7] active masks
+  int32_t *cur;               // [2][32] current priority per source (double-buffered)
+  int32_t *gmin;              // [2][32]
+  const int32_t *off, *dst, *w;
+  int32_t V;
+  int32_t delta;
+  uint32_t *bar;
+  int32_t *err;
+  uint64_t timeout_ns;
+  int32_t *stats;             // [0] iterations, [1] advances
+  int32_t *stop;              // raised by block 0 when the loop's time limit passes
+  uint64_t loop_limit_ns;
+};
+
+// Device buffers of one batched-SSSP pass; `owned` buffers are freed with it,
+// the others are the graph's reusable app slots.
+struct BsBuffers {
+  int32_t *dist = nullptr, *ints = nullptr, *out = nullptr, *dsrc = nullptr;
+  uint32_t *masks = nullptr;
+  int64_t *queues = nullptr;
+  int64_t qcap = 0;
+  bool owned = false;
+  ~BsBuffers();
+};
+gg_status bsssp_buffers(gg_graph *g, int32_t nsrc, bool owned, BsBuffers *b);
+BsState bsssp_state(gg_graph *g, const BsBuffers &b, int32_t delta);
+gg_status bsssp_enqueue(gg_graph *g, cudaStream_t st, const BsState &S, const int32_t *dsrc,
+                        int32_t k, int32_t *out_rows, bool timed);
+
+// ----------------------------------------------------------- batched BFS
+struct MsBfsState {
+  uint64_t *seen, *acc, *fr;  // V each
+  int32_t *qstamp;            // V: last level v was queued at
+  int32_t *q0, *q1;           // V each
+  int32_t *cnt3;              // rotating counts
+  int32_t *depth;             // [nsrc][V] (row-major per source)
+  int64_t depth_stride;       // V
+  int32_t nsrc;
+  uint32_t *bar;
+  int32_t *err;
+  uint64_t timeout_ns;
+  int32_t *stats;             // [0] levels
+  int32_t *stop;
+  uint64_t loop_limit_ns;
+};
+
+struct MsBfsBuffers {
+  uint64_t *masks = nullptr;
+  int32_t *ints = nullptr, *dsrc = nullptr;
+  bool owned = false;
+  ~MsBfsBuffers();
+};
+gg_status msbfs_buffers(gg_graph *g, int32_t nsrc, bool owned, MsBfsBuffers *b);
+MsBfsState msbfs_state(gg_graph *g, const MsBfsBuffers &b, int32_t k, int32_t *depth_rows);
+gg_status msbfs_enqueue(gg_graph *g, cudaStream_t st, const MsBfsState &S, const int32_t *dsrc,
+                        bool timed);
+
+}  // namespace gg

@@ -13,26 +13,10 @@
 // a source's bit enters seen[v] exactly at the first level that reaches v.
 #include <vector>
 
-#include "engine.h"
+#include "batch.h"
 #include "lb.cuh"
 
 namespace gg {
-
-struct MsBfsState {
-  uint64_t *seen, *acc, *fr;  // V each
-  int32_t *qstamp;            // V: last level v was queued at
-  int32_t *q0, *q1;           // V each
-  int32_t *cnt3;              // rotating counts
-  int32_t *depth;             // [nsrc][V] (row-major per source), may be null
-  int64_t depth_stride;       // V
-  int32_t nsrc;
-  uint32_t *bar;
-  int32_t *err;
-  uint64_t timeout_ns;
-  int32_t *stats;             // [0] levels
-  int32_t *stop;
-  uint64_t loop_limit_ns;
-};
 
 // Edge functor for the relax phase.
 struct UMsBfs {
@@ -141,6 +125,75 @@ __global__ void k_msbfs_seed(MsBfsState st, const int32_t *__restrict__ srcs) {
   *st.stop = 0;
 }
 
+// ------------------------------------------------------------------ host
+MsBfsBuffers::~MsBfsBuffers() {
+  if (owned)
+    for (void *p : {(void *)masks, (void *)ints, (void *)dsrc})
+      if (p) cudaFree(p);
+}
+
+gg_status msbfs_buffers(gg_graph *g, int32_t nsrc, bool owned, MsBfsBuffers *b) {
+  const int32_t V = g->csr.V;
+  b->owned = owned;
+  const size_t sz[3] = {sizeof(uint64_t) * 3 * (size_t)V, sizeof(int32_t) * (3 * (size_t)V + 64),
+                        sizeof(int32_t) * (size_t)std::max(nsrc, kMsBfsWidth)};
+  void **ptr[3] = {(void **)&b->masks, (void **)&b->ints, (void **)&b->dsrc};
+  for (int i = 0; i < 3; ++i) {
+    if (owned)
+      GG_CUDA(cudaMalloc(ptr[i], sz[i]));
+    else
+      GG_TRY(scratch_get_app(g, i, sz[i], ptr[i]));
+  }
+  return GG_OK;
+}
+
+MsBfsState msbfs_state(gg_graph *g, const MsBfsBuffers &b, int32_t k, int32_t *depth_rows) {
+  const int32_t V = g->csr.V;
+  MsBfsState S{};
+  S.seen = b.masks;
+  S.acc = b.masks + V;
+  S.fr = b.masks + 2 * (size_t)V;
+  S.qstamp = b.ints;
+  S.q0 = b.ints + V;
+  S.q1 = b.ints + 2 * (size_t)V;
+  S.cnt3 = b.ints + 3 * (size_t)V;
+  S.stats = b.ints + 3 * (size_t)V + 8;
+  S.stop = b.ints + 3 * (size_t)V + 12;
+  S.loop_limit_ns = loop_timeout_ns();
+  S.depth = depth_rows;
+  S.depth_stride = V;
+  S.nsrc = k;
+  S.bar = g->d_bar;
+  S.err = g->d_err;
+  S.timeout_ns = barrier_timeout_ns();
+  return S;
+}
+
+// One pass of k <= 64 sources: reset, seed, the persistent loop writing the
+// depth rows.  Stream-ordered only, so it can be captured into a CUDA graph.
+gg_status msbfs_enqueue(gg_graph *g, cudaStream_t st, const MsBfsState &S, const int32_t *dsrc,
+                        bool timed) {
+  int per_sm = 0;
+  const int cta = 512;
+  const size_t smem = twce_smem_bytes(cta);
+  GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_msbfs, cta, smem));
+  if (per_sm < 1) return set_error(GG_ERR_UNSUPPORTED, "batched BFS kernel does not fit an SM");
+  note_launch();
+  k_msbfs_init<<<g->sm_count * 8, 256, 0, st>>>(S, g->csr.V, dsrc);
+  note_launch();
+  k_msbfs_seed<<<1, 32, 0, st>>>(S, dsrc);
+  GG_CUDA(cudaMemsetAsync(S.bar, 0, sizeof(uint32_t) * 2, st));
+  DGraph dg = g->csr.view();
+  dg.nbuckets = 0;
+  MsBfsState arg = S;
+  void *args[] = {&dg, &arg};
+  if (timed) GG_CUDA(cudaEventRecord(g->ev2, st));
+  note_launch();
+  GG_CUDA(cudaLaunchCooperativeKernel((const void *)k_msbfs, per_sm * g->sm_count, cta, args, smem, st));
+  if (timed) GG_CUDA(cudaEventRecord(g->ev3, st));
+  return GG_OK;
+}
+
 }  // namespace gg
 
 using namespace gg;
@@ -148,60 +201,25 @@ using namespace gg;
 // Batched BFS: depth_out[s*V + v] for nsrc sources (host or device memory).
 extern "C" gg_status gg_bfs_batch(gg_graph *g, const int32_t *sources, int32_t nsrc,
                                   int32_t *depth_out, gg_stats *stats) {
-  GG_CHECK_ARG(g && sources && nsrc > 0, "bad arguments");
+  GG_CHECK_ARG(g && sources && nsrc > 0 && depth_out, "bad arguments");
   const int32_t V = g->csr.V;
   for (int32_t i = 0; i < nsrc; ++i)
     GG_CHECK_ARG(sources[i] >= 0 && sources[i] < V, "source out of range");
   if (stats) *stats = gg_stats{};
   cudaStream_t st = g->stream;
-  // device arrays (reused across calls through the app slots)
-  uint64_t *masks = nullptr;
-  int32_t *ints = nullptr, *depth = nullptr, *dsrc = nullptr;
-  GG_TRY(scratch_get_app(g, 0, sizeof(uint64_t) * 3 * (size_t)V, (void **)&masks));
-  GG_TRY(scratch_get_app(g, 1, sizeof(int32_t) * (3 * (size_t)V + 64), (void **)&ints));
-  GG_TRY(scratch_get_app(g, 2, sizeof(int32_t) * std::min<int32_t>(nsrc, 64) * (size_t)V, (void **)&depth));
-  GG_TRY(scratch_get_app(g, 3, sizeof(int32_t) * 64, (void **)&dsrc));
-  int per_sm = 0;
-  const int cta = 512;
-  const size_t smem = twce_smem_bytes(cta);
-  GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_msbfs, cta, smem));
-  if (per_sm < 1) return set_error(GG_ERR_UNSUPPORTED, "batched BFS kernel does not fit an SM");
+  MsBfsBuffers b;
+  GG_TRY(msbfs_buffers(g, nsrc, false, &b));
+  int32_t *depth = nullptr;
+  GG_TRY(scratch_get_app(g, 3, sizeof(int32_t) * (size_t)std::min(nsrc, kMsBfsWidth) * V, (void **)&depth));
   const uint64_t l0 = launches();
   cudaEventRecord(g->ev0, st);
   float loop_ms = 0;
   int32_t levels = 0;
-  for (int32_t base = 0; base < nsrc; base += 64) {
-    const int32_t k = std::min(64, nsrc - base);
-    MsBfsState S{};
-    S.seen = masks;
-    S.acc = masks + V;
-    S.fr = masks + 2 * (size_t)V;
-    S.qstamp = ints;
-    S.q0 = ints + V;
-    S.q1 = ints + 2 * (size_t)V;
-    S.cnt3 = ints + 3 * (size_t)V;
-    S.stats = ints + 3 * (size_t)V + 8;
-    S.stop = ints + 3 * (size_t)V + 12;
-    S.loop_limit_ns = loop_timeout_ns();
-    S.depth = depth;
-    S.depth_stride = V;
-    S.nsrc = k;
-    S.bar = g->d_bar;
-    S.err = g->d_err;
-    S.timeout_ns = barrier_timeout_ns();
-    GG_CUDA(cudaMemcpyAsync(dsrc, sources + base, sizeof(int32_t) * k, cudaMemcpyDefault, st));
-    note_launch();
-    k_msbfs_init<<<g->sm_count * 8, 256, 0, st>>>(S, V, dsrc);
-    note_launch();
-    k_msbfs_seed<<<1, 32, 0, st>>>(S, dsrc);
-    GG_CUDA(cudaMemsetAsync(g->d_bar, 0, sizeof(uint32_t) * 2, st));
-    DGraph dg = g->csr.view();
-    dg.nbuckets = 0;
-    void *args[] = {&dg, &S};
-    cudaEventRecord(g->ev2, st);
-    note_launch();
-    GG_CUDA(cudaLaunchCooperativeKernel((const void *)k_msbfs, per_sm * g->sm_count, cta, args, smem, st));
-    cudaEventRecord(g->ev3, st);
+  for (int32_t base = 0; base < nsrc; base += kMsBfsWidth) {
+    const int32_t k = std::min(kMsBfsWidth, nsrc - base);
+    const MsBfsState S = msbfs_state(g, b, k, depth);
+    GG_CUDA(cudaMemcpyAsync(b.dsrc, sources + base, sizeof(int32_t) * k, cudaMemcpyDefault, st));
+    GG_TRY(msbfs_enqueue(g, st, S, b.dsrc, true));
     GG_CUDA(cudaMemcpyAsync(depth_out + (size_t)base * V, depth, sizeof(int32_t) * (size_t)k * V,
                             cudaMemcpyDefault, st));
     GG_CUDA(cudaMemcpyAsync(g->h_pinned + 30, S.stats, sizeof(int32_t), cudaMemcpyDeviceToHost, st));

@@ -21,37 +21,16 @@
 // barrier | [advance pass 1 (minima) | barrier | pass 2 (move/keep) | barrier].
 #include <algorithm>
 
-#include "engine.h"
+#include "batch.h"
 
 namespace gg {
 
 constexpr int32_t kChunk = 256;  // edges per queue entry
-constexpr int32_t kLanes = 32;
+constexpr int32_t kLanes = kBsLanes;
 constexpr int32_t kPrefetch = 8;  // distance lines in flight per warp
 // Queue entries active for at most this many sources are relaxed edge-parallel
 // (lanes = edges); busier ones source-parallel (lanes = sources).
 constexpr int32_t kEdgeParallelMax = 6;
-
-struct BsState {
-  int32_t *dist;            // [V][32]
-  uint32_t *fr, *nacc, *far;  // [V] masks
-  int32_t *qstamp;          // [V]
-  int64_t *q[2];            // queue entries (u << 32 | chunk)
-  int64_t qcap;
-  int32_t *fl[2];           // far lists
-  int32_t *cnt;             // [0..2] queue counts (rotating), [3..4] far counts, [5..7] active masks
-  int32_t *cur;             // [2][32] current priority per source (double-buffered)
-  int32_t *gmin;            // [2][32]
-  const int32_t *off, *dst, *w;
-  int32_t V;
-  int32_t delta;
-  uint32_t *bar;
-  int32_t *err;
-  uint64_t timeout_ns;
-  int32_t *stats;           // [0] iterations, [1] advances
-  int32_t *stop;            // raised by block 0 when the loop's time limit passes
-  uint64_t loop_limit_ns;
-};
 
 __device__ __forceinline__ void bs_enqueue(const BsState &S, int64_t *q, int32_t *qcnt, int32_t v) {
   const int32_t deg = S.off[v + 1] - S.off[v];
@@ -341,6 +320,89 @@ __global__ void k_bsssp_out(const int32_t *__restrict__ dist, int32_t V, int32_t
   }
 }
 
+// ------------------------------------------------------------------ host
+BsBuffers::~BsBuffers() {
+  if (owned)
+    for (void *p : {(void *)dist, (void *)masks, (void *)ints, (void *)queues, (void *)out, (void *)dsrc})
+      if (p) cudaFree(p);
+}
+
+gg_status bsssp_buffers(gg_graph *g, int32_t nsrc, bool owned, BsBuffers *b) {
+  const int32_t V = g->csr.V;
+  const int64_t E = g->csr.E;
+  b->qcap = (int64_t)V + E / kChunk + 64;
+  b->owned = owned;
+  const size_t sz[6] = {sizeof(int32_t) * (size_t)V * kLanes, sizeof(uint32_t) * 3 * (size_t)V,
+                        sizeof(int32_t) * (3 * (size_t)V + 256), sizeof(int64_t) * 2 * (size_t)b->qcap,
+                        sizeof(int32_t) * (size_t)std::min(nsrc, kLanes) * V,
+                        sizeof(int32_t) * (size_t)std::max(nsrc, kLanes)};
+  void **ptr[6] = {(void **)&b->dist, (void **)&b->masks, (void **)&b->ints, (void **)&b->queues,
+                   (void **)&b->out, (void **)&b->dsrc};
+  for (int i = 0; i < 6; ++i) {
+    if (owned)
+      GG_CUDA(cudaMalloc(ptr[i], sz[i]));
+    else
+      GG_TRY(scratch_get_app(g, i, sz[i], ptr[i]));
+  }
+  return GG_OK;
+}
+
+BsState bsssp_state(gg_graph *g, const BsBuffers &b, int32_t delta) {
+  const int32_t V = g->csr.V;
+  BsState S{};
+  S.dist = b.dist;
+  S.fr = b.masks;
+  S.nacc = b.masks + V;
+  S.far = b.masks + 2 * (size_t)V;
+  S.qstamp = b.ints;
+  S.fl[0] = b.ints + V;
+  S.fl[1] = b.ints + 2 * (size_t)V;
+  int32_t *hdr = b.ints + 3 * (size_t)V;
+  S.cnt = hdr;              // 8
+  S.cur = hdr + 8;          // 64
+  S.gmin = hdr + 72;        // 64
+  S.stats = hdr + 136;      // 2
+  S.stop = hdr + 140;
+  S.q[0] = b.queues;
+  S.q[1] = b.queues + b.qcap;
+  S.qcap = b.qcap;
+  S.off = g->csr.off;
+  S.dst = g->csr.dst;
+  S.w = g->csr.w;
+  S.V = V;
+  S.delta = delta;
+  S.bar = g->d_bar;
+  S.err = g->d_err;
+  S.timeout_ns = barrier_timeout_ns();
+  S.loop_limit_ns = loop_timeout_ns();
+  return S;
+}
+
+// One group of k <= 32 sources (device array dsrc): reset, seed, the
+// persistent loop, and the per-source rows into out_rows.  Issues only
+// stream-ordered work, so it can be captured into a CUDA graph.
+gg_status bsssp_enqueue(gg_graph *g, cudaStream_t st, const BsState &S, const int32_t *dsrc, int32_t k,
+                        int32_t *out_rows, bool timed) {
+  int per_sm = 0;
+  GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bsssp, 256, 0));
+  if (per_sm < 1) return set_error(GG_ERR_UNSUPPORTED, "batched SSSP kernel does not fit an SM");
+  note_launch();
+  k_bsssp_init<<<g->sm_count * 8, 256, 0, st>>>(S, dsrc, k);
+  note_launch();
+  k_bsssp_seed<<<1, 32, 0, st>>>(S, dsrc, k);
+  GG_CUDA(cudaMemsetAsync(S.bar, 0, sizeof(uint32_t) * 2, st));
+  BsState arg = S;
+  void *args[] = {&arg};
+  if (timed) GG_CUDA(cudaEventRecord(g->ev2, st));
+  note_launch();
+  GG_CUDA(cudaLaunchCooperativeKernel((const void *)k_bsssp, per_sm * g->sm_count, 256, args, 0, st));
+  if (timed) GG_CUDA(cudaEventRecord(g->ev3, st));
+  note_launch();
+  k_bsssp_out<<<g->sm_count * 8, 256, 0, st>>>(S.dist, S.V, k, out_rows);
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
 }  // namespace gg
 
 using namespace gg;
@@ -351,71 +413,22 @@ extern "C" gg_status gg_sssp_batch(gg_graph *g, const int32_t *sources, int32_t 
   GG_CHECK_ARG(g && sources && nsrc > 0 && dist_out, "bad arguments");
   GG_CHECK_ARG(delta >= 1, "delta must be >= 1");
   const int32_t V = g->csr.V;
-  const int64_t E = g->csr.E;
   for (int32_t i = 0; i < nsrc; ++i)
     GG_CHECK_ARG(sources[i] >= 0 && sources[i] < V, "source out of range");
   if (stats) *stats = gg_stats{};
   cudaStream_t st = g->stream;
-  const int64_t qcap = (int64_t)V + E / kChunk + 64;
-  int32_t *dist = nullptr, *ints = nullptr, *out = nullptr, *dsrc = nullptr;
-  uint32_t *masks = nullptr;
-  int64_t *queues = nullptr;
-  GG_TRY(scratch_get_app(g, 0, sizeof(int32_t) * (size_t)V * kLanes, (void **)&dist));
-  GG_TRY(scratch_get_app(g, 1, sizeof(uint32_t) * 3 * (size_t)V, (void **)&masks));
-  GG_TRY(scratch_get_app(g, 2, sizeof(int32_t) * (3 * (size_t)V + 256), (void **)&ints));
-  GG_TRY(scratch_get_app(g, 3, sizeof(int64_t) * 2 * (size_t)qcap, (void **)&queues));
-  GG_TRY(scratch_get_app(g, 4, sizeof(int32_t) * (size_t)std::min(nsrc, kLanes) * V, (void **)&out));
-  GG_TRY(scratch_get_app(g, 5, sizeof(int32_t) * kLanes, (void **)&dsrc));
-  BsState S{};
-  S.dist = dist;
-  S.fr = masks;
-  S.nacc = masks + V;
-  S.far = masks + 2 * (size_t)V;
-  S.qstamp = ints;
-  S.fl[0] = ints + V;
-  S.fl[1] = ints + 2 * (size_t)V;
-  int32_t *hdr = ints + 3 * (size_t)V;
-  S.cnt = hdr;              // 8
-  S.cur = hdr + 8;          // 64
-  S.gmin = hdr + 72;        // 64
-  S.stats = hdr + 136;      // 2
-  S.stop = hdr + 140;
-  S.q[0] = queues;
-  S.q[1] = queues + qcap;
-  S.qcap = qcap;
-  S.off = g->csr.off;
-  S.dst = g->csr.dst;
-  S.w = g->csr.w;
-  S.V = V;
-  S.delta = delta;
-  S.bar = g->d_bar;
-  S.err = g->d_err;
-  S.timeout_ns = barrier_timeout_ns();
-  S.loop_limit_ns = loop_timeout_ns();
-  int per_sm = 0;
-  GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bsssp, 256, 0));
-  if (per_sm < 1) return set_error(GG_ERR_UNSUPPORTED, "batched SSSP kernel does not fit an SM");
+  BsBuffers b;
+  GG_TRY(bsssp_buffers(g, nsrc, false, &b));
+  const BsState S = bsssp_state(g, b, delta);
   const uint64_t l0 = launches();
   cudaEventRecord(g->ev0, st);
   float loop_ms = 0;
   int32_t iters = 0, advs = 0;
   for (int32_t base = 0; base < nsrc; base += kLanes) {
     const int32_t k = std::min(kLanes, nsrc - base);
-    GG_CUDA(cudaMemcpyAsync(dsrc, sources + base, sizeof(int32_t) * k, cudaMemcpyDefault, st));
-    note_launch();
-    k_bsssp_init<<<g->sm_count * 8, 256, 0, st>>>(S, dsrc, k);
-    note_launch();
-    k_bsssp_seed<<<1, 32, 0, st>>>(S, dsrc, k);
-    GG_CUDA(cudaMemsetAsync(g->d_bar, 0, sizeof(uint32_t) * 2, st));
-    void *args[] = {&S};
-    cudaEventRecord(g->ev2, st);
-    note_launch();
-    GG_CUDA(cudaLaunchCooperativeKernel((const void *)k_bsssp, per_sm * g->sm_count, 256, args, 0, st));
-    cudaEventRecord(g->ev3, st);
-    note_launch();
-    k_bsssp_out<<<g->sm_count * 8, 256, 0, st>>>(dist, V, k, out);
-    GG_CUDA(cudaGetLastError());
-    GG_CUDA(cudaMemcpyAsync(dist_out + (size_t)base * V, out, sizeof(int32_t) * (size_t)k * V,
+    GG_CUDA(cudaMemcpyAsync(b.dsrc, sources + base, sizeof(int32_t) * k, cudaMemcpyDefault, st));
+    GG_TRY(bsssp_enqueue(g, st, S, b.dsrc, k, b.out, true));
+    GG_CUDA(cudaMemcpyAsync(dist_out + (size_t)base * V, b.out, sizeof(int32_t) * (size_t)k * V,
                             cudaMemcpyDefault, st));
     GG_CUDA(cudaMemcpyAsync(g->h_pinned + 30, S.stats, sizeof(int32_t) * 2, cudaMemcpyDeviceToHost, st));
     GG_CUDA(cudaStreamSynchronize(st));

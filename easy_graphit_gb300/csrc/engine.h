@@ -164,9 +164,9 @@ int32_t pq_cutoff(const gg_pq *pq);
 // *ran is false when the schedule has no device-side form (the caller then
 // runs the loop unfused).
 bool fused_supported(const gg_schedule *s);
-gg_status fused_bfs(gg_graph *g, const gg_schedule *s, int32_t src, const VData &vd,
+gg_status fused_bfs(gg_graph *g, const gg_schedule *s, int32_t n0, const VData &vd,
                     gg_frontier *f, int32_t *iters, bool *ran);
-gg_status fused_sssp(gg_graph *g, const gg_schedule *s, int32_t src, int32_t delta, const VData &vd,
+gg_status fused_sssp(gg_graph *g, const gg_schedule *s, int32_t n0, int32_t delta, const VData &vd,
                      gg_frontier *f, int32_t *iters, int64_t *advances, bool *ran);
 uint64_t barrier_timeout_ns();
 uint64_t loop_timeout_ns();  // wall-clock bound of one persistent loop (GG_LOOP_TIMEOUT_MS)

@@ -237,10 +237,10 @@ static FusedArgs make_args(gg_graph *g, gg_frontier *f, const VData &vd) {
   return a;
 }
 
-// Counts start as {1 (the source), 0, 0}; both minima slots at INT_MAX.
-static gg_status init_counts(gg_graph *g) {
+// Counts start as {n0 (the sources), 0, 0}; both minima slots at INT_MAX.
+static gg_status init_counts(gg_graph *g, int32_t n0) {
   int32_t *h = g->h_pinned + 40;
-  h[0] = 1;
+  h[0] = n0;
   h[1] = 0;
   h[2] = 0;
   h[3] = 0;
@@ -262,11 +262,11 @@ static gg_status read_stats(gg_graph *g, int32_t *iters, int64_t *adv) {
   return GG_OK;
 }
 
-gg_status fused_bfs(gg_graph *g, const gg_schedule *s, int32_t, const VData &vd, gg_frontier *f,
+gg_status fused_bfs(gg_graph *g, const gg_schedule *s, int32_t n0, const VData &vd, gg_frontier *f,
                     int32_t *iters, bool *ran) {
   *ran = false;
   if (!fused_supported(s)) return GG_OK;
-  GG_TRY(init_counts(g));
+  GG_TRY(init_counts(g, n0));
   FusedArgs a = make_args(g, f, vd);
   const int cta = s->cta_size;
   const size_t sm = lb_smem(s->load_balancing, cta);
@@ -281,11 +281,11 @@ gg_status fused_bfs(gg_graph *g, const gg_schedule *s, int32_t, const VData &vd,
   return GG_OK;
 }
 
-gg_status fused_sssp(gg_graph *g, const gg_schedule *s, int32_t, int32_t delta, const VData &vd,
+gg_status fused_sssp(gg_graph *g, const gg_schedule *s, int32_t n0, int32_t delta, const VData &vd,
                      gg_frontier *f, int32_t *iters, int64_t *advances, bool *ran) {
   *ran = false;
   if (!fused_supported(s)) return GG_OK;
-  GG_TRY(init_counts(g));
+  GG_TRY(init_counts(g, n0));
   FusedArgs a = make_args(g, f, vd);
   a.delta = delta;
   const int cta = s->cta_size;

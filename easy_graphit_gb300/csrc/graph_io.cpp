@@ -446,6 +446,42 @@ gg_status gg_host_graph_save_bin(const gg_host_graph *g, const char *path) {
   return GG_OK;
 }
 
+gg_status gg_host_graph_union(const gg_host_graph *const *parts, int32_t n, int32_t *vertex_offsets,
+                              gg_host_graph **out) {
+  GG_CHECK_ARG(parts && n >= 1 && out, "bad arguments");
+  int64_t V = 0, E = 0;
+  for (int32_t i = 0; i < n; ++i) {
+    GG_CHECK_ARG(parts[i], "NULL part");
+    V += parts[i]->V;
+    E += parts[i]->E;
+  }
+  if (V >= INT32_MAX || E > INT32_MAX)
+    return gg::set_error(GG_ERR_INVALID, "union of %d graphs exceeds the int32 CSR layout", n);
+  auto *g = new (std::nothrow) gg_host_graph();
+  if (!g) return gg::set_error(GG_ERR_OOM, "host graph allocation failed");
+  g->V = (int32_t)V;
+  g->E = E;
+  g->offsets.resize(V + 1);
+  g->dst.resize(E);
+  g->w.resize(E);
+  int32_t vb = 0, eb = 0;
+  for (int32_t i = 0; i < n; ++i) {
+    const gg_host_graph *p = parts[i];
+    if (vertex_offsets) vertex_offsets[i] = vb;
+    for (int32_t v = 0; v < p->V; ++v) g->offsets[vb + v] = eb + p->offsets[v];
+    for (int64_t e = 0; e < p->E; ++e) {
+      g->dst[eb + e] = vb + p->dst[e];
+      g->w[eb + e] = p->w[e];
+    }
+    vb += p->V;
+    eb += (int32_t)p->E;
+  }
+  g->offsets[V] = eb;
+  if (vertex_offsets) vertex_offsets[n] = vb;
+  *out = g;
+  return GG_OK;
+}
+
 gg_status gg_host_graph_pick_sources(const gg_host_graph *g, int32_t n, int64_t seed, int32_t *out) {
   GG_CHECK_ARG(g && out && n >= 0, "bad arguments");
   if (g->E == 0) return gg::set_error(GG_ERR_INVALID, "graph has no edges to pick sources from");

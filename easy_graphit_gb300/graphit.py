@@ -277,6 +277,15 @@ class HostGraph:
     def out_degrees(self) -> np.ndarray:
         return np.diff(self.offsets)
 
+    @classmethod
+    def union(cls, parts) -> tuple["HostGraph", np.ndarray]:
+        """Disjoint union; returns (graph, vertex_offsets[len(parts)+1])."""
+        arr = (C.c_void_p * len(parts))(*[p._h for p in parts])
+        offs = np.empty(len(parts) + 1, dtype=np.int32)
+        h = C.c_void_p()
+        call("gg_host_graph_union", arr, len(parts), _np_ptr(offs), C.byref(h))
+        return cls(h), offs
+
     def pick_sources(self, n: int, seed: int = K_RAND_SEED) -> np.ndarray:
         """GAPBS SourcePicker (benchmark.h:50-71): n non-zero-degree vertices."""
         out = np.empty(n, dtype=np.int32)
@@ -480,6 +489,76 @@ def sssp_batch(g: GraphT, sources, delta: int, out=None):
     st = L.gg_stats()
     call("gg_sssp_batch", g.handle, _np_ptr(srcs), len(srcs), delta, _ptr(out), C.byref(st))
     return out, _stats(st)
+
+
+class BatchPlan:
+    """A batched BFS ("bfs") or SSSP ("sssp") captured into a CUDA graph once and
+    replayed by run().  `out` is a CUDA tensor of shape [nsrc, V] (int32)."""
+
+    def __init__(self, g: GraphT, app: str, sources, out, delta: int = 32):
+        self.g = g
+        srcs = np.ascontiguousarray(sources, dtype=np.int32)
+        h = C.c_void_p()
+        call("gg_batch_plan_create", g.handle, {"bfs": 0, "sssp": 1}[app], _np_ptr(srcs), len(srcs),
+             delta, _ptr(out), C.byref(h))
+        self._h = h
+
+    def run(self) -> dict:
+        st = L.gg_stats()
+        call("gg_batch_plan_run", self._h, C.byref(st))
+        return _stats(st)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gg_batch_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def bfs_multi(g: GraphT, sources, schedule=None, fuse=None):
+    """Multi-source BFS (distance to the nearest source): (depth, stats)."""
+    srcs = np.ascontiguousarray(sources, dtype=np.int32)
+    depth = np.empty(g.num_vertices, dtype=np.int32)
+    st = L.gg_stats()
+    a = _resolve("bfs", schedule, fuse)
+    call("gg_bfs_multi", g.handle, C.byref(a), _np_ptr(srcs), len(srcs), _ptr(depth), None,
+         C.byref(st))
+    return depth, _stats(st)
+
+
+def sssp_multi(g: GraphT, sources, delta: int, schedule=None, fuse=None):
+    """Multi-source delta-stepping SSSP: (dist, stats)."""
+    srcs = np.ascontiguousarray(sources, dtype=np.int32)
+    dist = np.empty(g.num_vertices, dtype=np.int32)
+    st = L.gg_stats()
+    a = _resolve("sssp", schedule, fuse)
+    call("gg_sssp_multi", g.handle, C.byref(a), _np_ptr(srcs), len(srcs), delta, _ptr(dist),
+         C.byref(st))
+    return dist, _stats(st)
+
+
+def multigraph_batch(parts, app: str, local_sources, delta: int = 32, schedule=None, fuse=True):
+    """Runs BFS or SSSP on many graphs of uneven size in one traversal: the
+    graphs become one disjoint union, each contributes its source, and the
+    union is traversed once.  Returns (list of per-graph results, stats)."""
+    hg, offs = HostGraph.union(parts)
+    g = GraphT(hg)
+    srcs = np.array([offs[i] + int(s) for i, s in enumerate(local_sources)], dtype=np.int32)
+    if schedule is None:
+        schedule = SimpleGPUSchedule().configLoadBalancing(SimpleGPUSchedule.load_balancing_type.TWCE)
+    if app == "bfs":
+        out, st = bfs_multi(g, srcs, schedule, fuse)
+    elif app == "sssp":
+        out, st = sssp_multi(g, srcs, delta, schedule, fuse)
+    else:
+        raise ValueError(app)
+    g.close()
+    return [out[offs[i]:offs[i + 1]] for i in range(len(parts))], st
 
 
 def bc(g: GraphT, src: int, schedule=None, fuse=None):

@@ -137,6 +137,12 @@ gg_status gg_host_graph_load(const char *path, int32_t symmetrize,
 gg_status gg_host_graph_save_bin(const gg_host_graph *g, const char *path);
 gg_status gg_host_graph_info(const gg_host_graph *g, int32_t *num_vertices,
                              int64_t *num_edges);
+/* Disjoint union of n host graphs (part i's vertex v becomes
+ * vertex_offsets[i] + v; vertex_offsets may be NULL, else n+1 entries).  Used
+ * to run many graphs of uneven size in one traversal (gg_bfs_multi /
+ * gg_sssp_multi with one source per part). */
+gg_status gg_host_graph_union(const gg_host_graph *const *parts, int32_t n,
+                              int32_t *vertex_offsets, gg_host_graph **out);
 /* n sources as GAPBS's SourcePicker draws them (infra_gapbs/benchmark.h:50-71):
  * uniform ids from std::mt19937(seed), skipping vertices with no out-edges. */
 gg_status gg_host_graph_pick_sources(const gg_host_graph *g, int32_t n,
@@ -342,6 +348,27 @@ gg_status gg_bfs_noalloc(const int32_t *offsets, const int32_t *dst,
  *    scans; dist_out[s*V + v] (INT_MAX unreached). */
 gg_status gg_bfs_batch(gg_graph *g, const int32_t *sources, int32_t nsrc,
                        int32_t *depth_out, gg_stats *stats);
+/* Batch plans: a whole gg_bfs_batch / gg_sssp_batch captured once into a CUDA
+ * graph (every persistent launch of every group of sources) and replayed with
+ * one graph launch per run.  `out` must be device memory (nsrc*V int32); the
+ * plan copies the sources and owns its device state. */
+typedef struct gg_batch_plan gg_batch_plan;
+enum { GG_BATCH_BFS = 0, GG_BATCH_SSSP = 1 };
+gg_status gg_batch_plan_create(gg_graph *g, int32_t app, const int32_t *sources,
+                               int32_t nsrc, int32_t delta, int32_t *out,
+                               gg_batch_plan **plan);
+gg_status gg_batch_plan_run(gg_batch_plan *plan, gg_stats *stats);
+gg_status gg_batch_plan_destroy(gg_batch_plan *plan);
+/* Multi-source traversal with the app schedule: every source starts at 0 and
+ * out[v] is the distance to the nearest source.  With one source per part of a
+ * gg_host_graph_union this runs many graphs of uneven size in one persistent
+ * launch (fuse=1), load-balanced across graphs by the schedule's LB. */
+gg_status gg_bfs_multi(gg_graph *g, const gg_app_schedule *s,
+                       const int32_t *sources, int32_t n, int32_t *depth_out,
+                       int32_t *parent_out, gg_stats *stats);
+gg_status gg_sssp_multi(gg_graph *g, const gg_app_schedule *s,
+                        const int32_t *sources, int32_t n, int32_t delta,
+                        int32_t *dist_out, gg_stats *stats);
 gg_status gg_sssp_batch(gg_graph *g, const int32_t *sources, int32_t nsrc,
                         int32_t delta, int32_t *dist_out, gg_stats *stats);
 

@@ -69,3 +69,58 @@ def test_sssp_batch_larger_graph_device_output():
     got = out.cpu().numpy()
     for i in [0, 7, 31]:
         np.testing.assert_array_equal(got[i], oracle.sssp_dijkstra(off, dst, w, int(srcs[i])))
+
+
+# ------------------------------------------------ multi-source / multi-graph
+def test_multi_source_equals_min_over_sources():
+    from easy_graphit_gb300 import bfs_multi, sssp_multi
+    hg, g, (off, dst, w) = graph("dir14")
+    srcs = hg.pick_sources(7, seed=3)
+    depth, _ = bfs_multi(g, srcs)
+    bref = np.stack([oracle.bfs(off, dst, int(s)) for s in srcs]).astype(np.int64)
+    bref[bref < 0] = 2**40
+    bmin = bref.min(axis=0)
+    bmin[bmin == 2**40] = -1
+    np.testing.assert_array_equal(depth, bmin)
+    for delta in (1, 32):
+        dist, _ = sssp_multi(g, srcs, delta)
+        sref = np.stack([oracle.sssp_dijkstra(off, dst, w, int(s)) for s in srcs]).min(axis=0)
+        np.testing.assert_array_equal(dist, sref)
+
+
+@pytest.mark.parametrize("app", ["bfs", "sssp"])
+def test_multigraph_batch_uneven_graphs(app):
+    from easy_graphit_gb300 import multigraph_batch
+    rng = np.random.default_rng(27491095)
+    parts = []
+    for i in range(10):
+        if i % 3 == 2:
+            n = int(rng.integers(8, 40))
+            parts.append(HostGraph.grid(n, n, seed=100 + i))
+        else:
+            parts.append(HostGraph.rmat(int(rng.integers(6, 13)), int(rng.integers(4, 33)), seed=200 + i))
+    local = [int(p.pick_sources(1, seed=i)[0]) for i, p in enumerate(parts)]
+    res, st = multigraph_batch(parts, app, local, delta=16)
+    for p, s, r in zip(parts, local, res):
+        off, dst, w = np.array(p.offsets), np.array(p.dst), np.array(p.weights)
+        ref = oracle.bfs(off, dst, s) if app == "bfs" else oracle.sssp_dijkstra(off, dst, w, s)
+        np.testing.assert_array_equal(r, ref)
+
+
+@pytest.mark.parametrize("app", ["bfs", "sssp"])
+def test_batch_plan_cuda_graph_replay(app):
+    import torch
+    from easy_graphit_gb300 import BatchPlan
+    hg, g, (off, dst, w) = graph("dir14")
+    srcs = hg.pick_sources(70, seed=9)
+    out = torch.full((70, hg.num_vertices), -7, dtype=torch.int32, device="cuda")
+    plan = BatchPlan(g, app, srcs, out, delta=32)
+    for _ in range(2):  # replay twice: the second run must not see the first's state
+        st = plan.run()
+        got = out.cpu().numpy()
+        for i in [0, 33, 63, 64, 69]:
+            ref = oracle.bfs(off, dst, int(srcs[i])) if app == "bfs" else \
+                oracle.sssp_dijkstra(off, dst, w, int(srcs[i]))
+            np.testing.assert_array_equal(got[i], ref)
+        out.fill_(-7)
+    plan.close()

@@ -183,3 +183,15 @@ def test_errors_are_reported_not_fatal():
     st = L.lib().gg_host_graph_rmat(0, 16, 0.57, 0.19, 0.19, 1, 0, 1, 255, C.byref(h))
     assert st == L.GG_ERR_INVALID
     assert "scale" in L.last_error()
+
+
+def test_host_graph_union():
+    a = HostGraph.rmat(6, 4)
+    b = HostGraph.grid(3, 4)
+    u, offs = HostGraph.union([a, b])
+    assert list(offs) == [0, a.num_vertices, a.num_vertices + b.num_vertices]
+    assert u.num_edges == a.num_edges + b.num_edges
+    np.testing.assert_array_equal(u.dst[:a.num_edges], a.dst)
+    np.testing.assert_array_equal(u.dst[a.num_edges:], b.dst + a.num_vertices)
+    np.testing.assert_array_equal(u.weights[a.num_edges:], b.weights)
+    np.testing.assert_array_equal(np.diff(u.offsets), np.concatenate([np.diff(a.offsets), np.diff(b.offsets)]))
