@@ -208,6 +208,7 @@ def run_gb300(args):
 
     from easy_graphit_gb300 import GraphT, _lib as L, app_schedule, default_schedule
     from easy_graphit_gb300 import SimpleGPUSchedule as T
+    from easy_graphit_gb300.replicas import aggregate_teps, rank_sources
 
     rank, world, local = dist_env()
     if world > 1:
@@ -219,7 +220,7 @@ def run_gb300(args):
     off, dst, w = np.array(hg.offsets), np.array(hg.dst), np.array(hg.weights)
     V, E = hg.num_vertices, hg.num_edges
     # weak scaling: every rank traverses its own 32 sources on its own replica
-    sources = hg.pick_sources(N_SOURCES, seed=27491095 + rank)
+    sources = rank_sources(hg, N_SOURCES, rank)
     h_src = np.ascontiguousarray(sources, dtype=np.int32)
 
     g = GraphT(hg)
@@ -292,12 +293,9 @@ def run_gb300(args):
         torch.cuda.synchronize()
     launches = int(L.lib().gg_kernel_launches() - l0)
     ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    # whole job: edges of all ranks / the slowest rank's time (no data-path collective)
+    value, ms = aggregate_teps(total_edges * args.steps, ms, device=dev)
     ms_per_step = ms / args.steps
-    value = total_edges * world / (ms_per_step / 1e3) / 1e9
 
     # End to end through the C ABI with host buffers: upload the CSR from
     # pinned host memory, run the batch with distances written to pinned host
@@ -319,7 +317,7 @@ def run_gb300(args):
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
     assert np.array_equal(h_out.numpy(), dd)
-    e2e_val = total_edges * world / (e2e_ms / 1e3) / 1e9
+    e2e_val, e2e_ms = aggregate_teps(total_edges, e2e_ms, device=dev)
 
     if rank != 0:
         if world > 1:
