@@ -49,6 +49,17 @@ class gg_vertex_data(C.Structure):
                 ("damping", f32)]
 
 
+class gg_batch_tuning(C.Structure):
+    _fields_ = [("blocks_per_sm", i32), ("chunk", i32), ("edge_parallel_max", i32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class gg_tune_row(C.Structure):
+    _fields_ = [("tuning", gg_batch_tuning), ("ms", f32)]
+
+
 class gg_stats(C.Structure):
     _fields_ = [("iterations", i32), ("push_iterations", i32), ("pull_iterations", i32),
                 ("bucket_advances", i32), ("vertices_reached", i64), ("edges_traversed", i64),
@@ -116,12 +127,28 @@ SIGNATURES: dict[str, tuple] = {
     "gg_kernel_launches": (C.c_uint64, []),
     "gg_bfs_noalloc": (i32, [P, P, i32, i32, i32, P, P]),
     "gg_bfs_batch": (i32, [P, P, i32, P, C.POINTER(gg_stats)]),
+    "gg_bc_batch": (i32, [P, P, i32, P, C.POINTER(gg_stats)]),
     "gg_bfs_multi": (i32, [P, C.POINTER(gg_app_schedule), P, i32, P, P, C.POINTER(gg_stats)]),
     "gg_sssp_multi": (i32, [P, C.POINTER(gg_app_schedule), P, i32, i32, P, C.POINTER(gg_stats)]),
     "gg_host_graph_union": (i32, [P, i32, P, C.POINTER(P)]),
     "gg_batch_plan_create": (i32, [P, i32, P, i32, i32, P, C.POINTER(P)]),
     "gg_batch_plan_run": (i32, [P, C.POINTER(gg_stats)]),
     "gg_batch_plan_destroy": (i32, [P]),
+    "gg_batch_set_tuning": (i32, [P, i32, C.POINTER(gg_batch_tuning)]),
+    "gg_batch_get_tuning": (i32, [P, i32, C.POINTER(gg_batch_tuning)]),
+    "gg_batch_autotune": (i32, [P, i32, P, i32, i32, C.POINTER(gg_batch_tuning), P, i32,
+                                C.POINTER(i32)]),
+    "gg_selector_create": (i32, [i64, C.POINTER(P)]),
+    "gg_selector_destroy": (i32, [P]),
+    "gg_selector_num_params": (i32, []),
+    "gg_selector_get_params": (i32, [P, P, i32]),
+    "gg_selector_set_params": (i32, [P, P, i32]),
+    "gg_selector_forward": (i32, [P, P, i32, P]),
+    "gg_selector_grad": (i32, [P, P, P, i32, P, P]),
+    "gg_selector_train": (i32, [P, P, P, i32, i32, f32, P]),
+    "gg_selector_save": (i32, [P, C.c_char_p]),
+    "gg_selector_load": (i32, [C.c_char_p, C.POINTER(P)]),
+    "gg_selector_collect": (i32, [P, i32, i32, i32, i32, P, P, P]),
     "gg_sssp_batch": (i32, [P, P, i32, i32, P, C.POINTER(gg_stats)]),
 }
 

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "selector.h"
 
 namespace gg {
 
@@ -84,6 +85,39 @@ gg_status reach_stats(gg_graph *g, const int32_t *val, gg_stats *st) {
   st->edges_traversed = (int64_t)h[1];
   return GG_OK;
 }
+
+// The schedule of one iteration: the learned selector's choice when the app
+// schedule is GG_SCHED_LEARNED with a model (fallback s1 otherwise), else the
+// simple / hybrid rule.  `f` may be NULL for rounds over every vertex.
+struct Chooser {
+  gg_graph *g;
+  const gg_app_schedule *s;
+  RunTotals rt{};
+  gg_schedule learned{};
+  gg_status choose(gg_frontier *f, int32_t n, const gg_schedule **out) {
+    if (s->kind != GG_SCHED_LEARNED || !s->selector) {
+      *out = pick(s, n, g->csr.V);
+      return GG_OK;
+    }
+    FrontierStats fs;
+    if (f) {
+      GG_TRY(frontier_stats(g, f, &fs));
+    } else {
+      fs.n = g->csr.V;
+      fs.sum_deg = g->csr.E;
+    }
+    float x[kSelectorFeatures];
+    make_features(g, fs, rt, x);
+    int32_t d[3];
+    GG_TRY(selector_decide(const_cast<gg_selector *>(s->selector), x, d, g->stream));
+    learned = candidate_schedule(s->s1, d[0], d[1], d[2]);
+    *out = &learned;
+    rt.visited_v = std::min<double>(g->csr.V, rt.visited_v + fs.n);
+    rt.visited_e = std::min<double>(g->csr.E, rt.visited_e + fs.sum_deg);
+    rt.iteration++;
+    return GG_OK;
+  }
+};
 
 // CUDA events around one trial (and, when a loop recorded ev2/ev3, around its
 // traversal loop), plus the number of kernels the trial launched.
@@ -208,10 +242,12 @@ gg_status run_bfs(gg_graph *g, const gg_app_schedule *s, const int32_t *srcs, in
   }
   LoopTimer lt(g);
   int32_t n = 1;
+  Chooser ch{g, s};
   for (int32_t level = 1;; ++level) {
     GG_TRY(frontier_size(f, &n));
     if (n == 0) break;
-    const gg_schedule *sc = pick(s, n, V);
+    const gg_schedule *sc = nullptr;
+    GG_TRY(ch.choose(f, n, &sc));
     vd.level = level;
     GG_TRY(edgeset_apply_impl(g, sc, GG_UDF_BFS_PARENT, GG_FILTER_PARENT_UNSET, f, f, true, vd,
                               INT_MAX, false));
@@ -251,7 +287,7 @@ gg_status run_sssp(gg_graph *g, const gg_app_schedule *s, const int32_t *srcs, i
     }
   }
   LoopTimer lt(g);
-  const int32_t V = g->csr.V;
+  Chooser ch{g, s};
   for (;;) {
     bool fin = false;
     GG_TRY(pq_finished(pq, &fin));
@@ -259,7 +295,8 @@ gg_status run_sssp(gg_graph *g, const gg_app_schedule *s, const int32_t *srcs, i
     GG_TRY(pq_dequeue(pq));
     int32_t n = 0;
     GG_TRY(frontier_size(pq->frontier, &n));
-    const gg_schedule *sc = pick(s, n, V);
+    const gg_schedule *sc = nullptr;
+    GG_TRY(ch.choose(pq->frontier, n, &sc));
     GG_TRY(edgeset_apply_impl(g, sc, GG_UDF_SSSP_RELAX, GG_FILTER_NONE, pq->frontier, pq->frontier,
                               true, vd, pq_cutoff(pq), false));
     if (st) st->iterations++;
@@ -362,6 +399,24 @@ gg_status gg_pagerank(gg_graph *g, const gg_app_schedule *s, int32_t iters, floa
   const int32_t V = g->csr.V;
   if (st) *st = gg_stats{};
   float *old_rank = nullptr, *new_rank = nullptr, *contrib = nullptr;
+  if (s->kind == GG_SCHED_SIMPLE && s->s1.direction == GG_PULL && s->s1.load_balancing == GG_LB_TWC) {
+    // static pull gather: in-degree bins once, one owner per vertex, no atomics
+    GG_TRY(app_array(g, 3, V, &old_rank));
+    GG_TRY(app_array(g, 5, 2 * (size_t)V, &contrib));
+    Trial t(g);
+    GG_TRY(pagerank_pull_twc(g, iters, damping, old_rank, contrib));
+    GG_TRY(t.stop(st));
+    GG_TRY(check_device_error(g, "pagerank"));
+    if (rank_out) GG_CUDA(cudaMemcpyAsync(rank_out, old_rank, sizeof(float) * V, cudaMemcpyDefault, g->stream));
+    if (st) {
+      st->iterations = iters;
+      st->pull_iterations = iters;
+      st->vertices_reached = V;
+      st->edges_traversed = (int64_t)g->csr.E * iters;
+    }
+    GG_CUDA(cudaStreamSynchronize(g->stream));
+    return GG_OK;
+  }
   GG_TRY(app_array(g, 3, V, &old_rank));
   GG_TRY(app_array(g, 4, V, &new_rank));
   GG_TRY(app_array(g, 5, V, &contrib));
@@ -407,9 +462,11 @@ gg_status gg_cc(gg_graph *g, const gg_app_schedule *s, int32_t *labels_out, gg_s
   GG_TRY(vertexset_apply_impl(g, nullptr, GG_VUDF_CC_INIT, vd));
   hu[0] = 1;
   int32_t rounds = 0;
+  Chooser ch{g, s};
   while (hu[0]) {  // while (updates[0])
     GG_CUDA(cudaMemsetAsync(updates, 0, sizeof(int32_t), g->stream));
-    const gg_schedule *sc = pick(s, V, V);
+    const gg_schedule *sc = nullptr;
+    GG_TRY(ch.choose(nullptr, V, &sc));
     GG_TRY(edgeset_apply_impl(g, sc, GG_UDF_CC_HOOK, GG_FILTER_NONE, nullptr, nullptr, true, vd,
                               INT_MAX, false));
     count_dir(st, sc);

@@ -7,7 +7,40 @@
 namespace gg {
 
 constexpr int32_t kBsLanes = 32;  // sources per batched-SSSP pass (warp lanes)
+constexpr int32_t kMinChunk = 32;   // smallest work-item chunk (sizes the item queues)
+constexpr int32_t kMaxChunk = 4096;
+
+// A graph's tuning of one batched app with the defaults filled in;
+// blocks_per_sm capped at `fit` (CTAs of the kernel that fit one SM).
+inline gg_batch_tuning effective_tuning(const gg_graph *g, int32_t app, int fit) {
+  gg_batch_tuning t = g->tuning[app];
+  if (t.blocks_per_sm <= 0 || t.blocks_per_sm > fit) t.blocks_per_sm = fit;
+  if (t.chunk <= 0) t.chunk = 256;
+  if (t.edge_parallel_max == 0) t.edge_parallel_max = 6;
+  return t;
+}
 constexpr int32_t kMsBfsWidth = 64;  // sources per batched-BFS pass (mask bits)
+
+// Relax functor of the bit-parallel multi-source BFS (batched BFS and the
+// forward sweep of batched BC): acc[v] |= fr[u] & ~seen[v]; the first thread
+// to touch v at this level queues it.
+struct UMsBfs {
+  static constexpr bool kWeight = false;
+  const uint64_t *seen, *fr;
+  uint64_t *acc;
+  int32_t *qstamp;
+  int32_t level;
+  __device__ __forceinline__ bool src_ok(int32_t) const { return true; }
+  __device__ __forceinline__ bool dst_ok(int32_t) const { return true; }
+  __device__ __forceinline__ int32_t apply(int32_t u, int32_t v, int32_t) const {
+    const uint64_t nb = __ldcg(fr + u) & ~__ldcg(seen + v);
+    if (!nb) return -1;
+    if ((__ldcg(acc + v) & nb) == nb) return -1;  // nothing new for acc
+    atomicOr((unsigned long long *)(acc + v), (unsigned long long)nb);
+    if (atomicMax(qstamp + v, level) < level) return v;
+    return -1;
+  }
+};
 
 // ---------------------------------------------------------- batched SSSP
 struct BsState {
@@ -23,6 +56,8 @@ struct BsState {
   const int32_t *off, *dst, *w;
   int32_t V;
   int32_t delta;
+  int32_t chunk;              // edges per queue entry
+  int32_t ep_max;             // entries active for <= ep_max sources run edge-parallel
   uint32_t *bar;
   int32_t *err;
   uint64_t timeout_ns;
@@ -73,5 +108,28 @@ gg_status msbfs_buffers(gg_graph *g, int32_t nsrc, bool owned, MsBfsBuffers *b);
 MsBfsState msbfs_state(gg_graph *g, const MsBfsBuffers &b, int32_t k, int32_t *depth_rows);
 gg_status msbfs_enqueue(gg_graph *g, cudaStream_t st, const MsBfsState &S, const int32_t *dsrc,
                         bool timed);
+
+// ------------------------------------------------------------ batched BC
+// Device buffers of one batched-BC pass (64 sources); `owned` buffers are
+// freed with it, the others are the graph's reusable app slots.
+struct BcBuffers {
+  uint64_t *masks = nullptr;
+  int32_t *ints = nullptr, *dsrc = nullptr;
+  int64_t *work = nullptr;
+  uint16_t *depth = nullptr;
+  double *vals = nullptr;
+  size_t bytes_masks = 0, bytes_ints = 0, bytes_depth = 0, bytes_vals = 0;
+  bool owned = false;
+  ~BcBuffers();
+};
+gg_status bcb_buffers(gg_graph *g, bool owned, BcBuffers *b);
+
+// The persistent kernels (for occupancy queries).
+const void *bsssp_kernel();
+const void *msbfs_kernel();
+const void *bcb_kernel();
+gg_status bcb_enqueue(gg_graph *g, cudaStream_t st, const BcBuffers &b, int32_t k, const int32_t *dsrc,
+                      float *out, int64_t out_stride, unsigned long long *reached, int32_t *stats,
+                      bool timed);
 
 }  // namespace gg

@@ -18,26 +18,6 @@
 
 namespace gg {
 
-// Edge functor for the relax phase.
-struct UMsBfs {
-  static constexpr bool kWeight = false;
-  const uint64_t *seen, *fr;
-  uint64_t *acc;
-  int32_t *qstamp;
-  int32_t level;
-  __device__ __forceinline__ bool src_ok(int32_t) const { return true; }
-  __device__ __forceinline__ bool dst_ok(int32_t) const { return true; }
-  __device__ __forceinline__ int32_t apply(int32_t u, int32_t v, int32_t) const {
-    const uint64_t nb = __ldcg(fr + u) & ~__ldcg(seen + v);
-    if (!nb) return -1;
-    if ((__ldcg(acc + v) & nb) == nb) return -1;  // nothing new for acc
-    atomicOr((unsigned long long *)(acc + v), (unsigned long long)nb);
-    // first toucher this level queues v
-    if (atomicMax(qstamp + v, level) < level) return v;
-    return -1;
-  }
-};
-
 __global__ void __launch_bounds__(512) k_msbfs(DGraph g, MsBfsState st) {
   extern __shared__ int4 smem[];
   int32_t *qs[2] = {st.q0, st.q1};
@@ -169,6 +149,8 @@ MsBfsState msbfs_state(gg_graph *g, const MsBfsBuffers &b, int32_t k, int32_t *d
   return S;
 }
 
+const void *msbfs_kernel() { return (const void *)k_msbfs; }
+
 // One pass of k <= 64 sources: reset, seed, the persistent loop writing the
 // depth rows.  Stream-ordered only, so it can be captured into a CUDA graph.
 gg_status msbfs_enqueue(gg_graph *g, cudaStream_t st, const MsBfsState &S, const int32_t *dsrc,
@@ -189,7 +171,8 @@ gg_status msbfs_enqueue(gg_graph *g, cudaStream_t st, const MsBfsState &S, const
   void *args[] = {&dg, &arg};
   if (timed) GG_CUDA(cudaEventRecord(g->ev2, st));
   note_launch();
-  GG_CUDA(cudaLaunchCooperativeKernel((const void *)k_msbfs, per_sm * g->sm_count, cta, args, smem, st));
+  const int bps = effective_tuning(g, GG_BATCH_BFS, per_sm).blocks_per_sm;
+  GG_CUDA(cudaLaunchCooperativeKernel((const void *)k_msbfs, bps * g->sm_count, cta, args, smem, st));
   if (timed) GG_CUDA(cudaEventRecord(g->ev3, st));
   return GG_OK;
 }

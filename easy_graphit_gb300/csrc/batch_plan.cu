@@ -1,4 +1,4 @@
-// Batch plans: a whole batched BFS or SSSP (every pass of every group of
+// Batch plans: a whole batched BFS, SSSP or BC (every pass of every group of
 // sources) captured once into a CUDA graph and replayed with one
 // cudaGraphLaunch per step -- no host round trips, no per-kernel launch cost.
 // The plan owns its device state and its copy of the sources, and writes into
@@ -16,6 +16,8 @@ struct gg_batch_plan {
   int32_t ngroups = 0;
   gg::BsBuffers bs;
   gg::MsBfsBuffers ms;
+  gg::BcBuffers bc;
+  unsigned long long *reached = nullptr;  // BC: reached out-edges summed over sources
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int32_t launches_per_run = 0;
@@ -24,6 +26,7 @@ struct gg_batch_plan {
     if (graph) cudaGraphDestroy(graph);
     if (dsrc) cudaFree(dsrc);
     if (dstats) cudaFree(dstats);
+    if (reached) cudaFree(reached);
   }
 };
 
@@ -32,9 +35,9 @@ using namespace gg;
 extern "C" {
 
 gg_status gg_batch_plan_create(gg_graph *g, int32_t app, const int32_t *sources, int32_t nsrc,
-                               int32_t delta, int32_t *out, gg_batch_plan **plan) {
+                               int32_t delta, void *out, gg_batch_plan **plan) {
   GG_CHECK_ARG(g && sources && nsrc > 0 && out && plan, "bad arguments");
-  GG_CHECK_ARG(app == GG_BATCH_BFS || app == GG_BATCH_SSSP, "unknown batched app");
+  GG_CHECK_ARG(app == GG_BATCH_BFS || app == GG_BATCH_SSSP || app == GG_BATCH_BC, "unknown batched app");
   GG_CHECK_ARG(app != GG_BATCH_SSSP || delta >= 1, "delta must be >= 1");
   cudaPointerAttributes pa{};
   if (cudaPointerGetAttributes(&pa, out) != cudaSuccess || pa.type != cudaMemoryTypeDevice)
@@ -46,15 +49,19 @@ gg_status gg_batch_plan_create(gg_graph *g, int32_t app, const int32_t *sources,
   p->g = g;
   p->app = app;
   p->nsrc = nsrc;
-  const int32_t width = app == GG_BATCH_BFS ? kMsBfsWidth : kBsLanes;
+  const int32_t width = app == GG_BATCH_SSSP ? kBsLanes : kMsBfsWidth;
   p->ngroups = ceil_div(nsrc, width);
   GG_CUDA(cudaMalloc(&p->dsrc, sizeof(int32_t) * nsrc));
   GG_CUDA(cudaMemcpy(p->dsrc, sources, sizeof(int32_t) * nsrc, cudaMemcpyDefault));
   GG_CUDA(cudaMalloc(&p->dstats, sizeof(int32_t) * 2 * p->ngroups));
-  if (app == GG_BATCH_BFS)
+  if (app == GG_BATCH_BFS) {
     GG_TRY(msbfs_buffers(g, nsrc, true, &p->ms));
-  else
+  } else if (app == GG_BATCH_SSSP) {
     GG_TRY(bsssp_buffers(g, nsrc, true, &p->bs));
+  } else {
+    GG_TRY(bcb_buffers(g, true, &p->bc));
+    GG_CUDA(cudaMalloc(&p->reached, sizeof(unsigned long long)));
+  }
   // Capture on the graph's own stream (capturable even when the graph is
   // bound to a legacy default stream).
   cudaStream_t cs = g->own_stream;
@@ -62,17 +69,24 @@ gg_status gg_batch_plan_create(gg_graph *g, int32_t app, const int32_t *sources,
   const uint64_t l0 = launches();
   GG_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
   gg_status st = GG_OK;
+  if (app == GG_BATCH_BC) {
+    const cudaError_t me = cudaMemsetAsync(p->reached, 0, sizeof(unsigned long long), cs);
+    if (me != cudaSuccess) st = set_error(GG_ERR_CUDA, "memset in capture: %s", cudaGetErrorString(me));
+  }
   for (int32_t gi = 0; gi < p->ngroups && st == GG_OK; ++gi) {
     const int32_t base = gi * width;
     const int32_t k = std::min(width, nsrc - base);
     if (app == GG_BATCH_BFS) {
-      MsBfsState S = msbfs_state(g, p->ms, k, out + (size_t)base * V);
+      MsBfsState S = msbfs_state(g, p->ms, k, (int32_t *)out + (size_t)base * V);
       S.stats = p->dstats + 2 * gi;
       st = msbfs_enqueue(g, cs, S, p->dsrc + base, false);
-    } else {
+    } else if (app == GG_BATCH_SSSP) {
       BsState S = bsssp_state(g, p->bs, delta);
       S.stats = p->dstats + 2 * gi;
-      st = bsssp_enqueue(g, cs, S, p->dsrc + base, k, out + (size_t)base * V, false);
+      st = bsssp_enqueue(g, cs, S, p->dsrc + base, k, (int32_t *)out + (size_t)base * V, false);
+    } else {
+      st = bcb_enqueue(g, cs, p->bc, k, p->dsrc + base, (float *)out + (size_t)base * V, V, p->reached,
+                       p->dstats + 2 * gi, false);
     }
   }
   cudaGraph_t graph = nullptr;
@@ -107,6 +121,11 @@ gg_status gg_batch_plan_run(gg_batch_plan *p, gg_stats *stats) {
     for (int32_t gi = 0; gi < p->ngroups; ++gi) {
       stats->iterations = std::max(stats->iterations, h[2 * gi]);
       if (p->app == GG_BATCH_SSSP) stats->bucket_advances += h[2 * gi + 1];
+    }
+    if (p->app == GG_BATCH_BC) {
+      unsigned long long er = 0;
+      GG_CUDA(cudaMemcpy(&er, p->reached, sizeof(er), cudaMemcpyDeviceToHost));
+      stats->edges_traversed = 2 * (int64_t)er;
     }
     cudaEventElapsedTime(&stats->device_ms, g->ev0, g->ev1);
     stats->loop_ms = stats->device_ms;

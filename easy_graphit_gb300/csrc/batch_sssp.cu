@@ -3,7 +3,7 @@
 //
 // Layout: distances are vertex-major, dist[v*32 + s], so the 32 sources of a
 // vertex share one 128-byte line.  A warp owns one queue entry (a vertex u and
-// a chunk of at most kChunk of its edges); lane s relaxes source s.  For each
+// a chunk of at most S.chunk of its edges); lane s relaxes source s.  For each
 // edge the warp loads one line of dist[v][*] and issues atomicMin only where a
 // source improves, so an edge is read once for all sources that have u on their
 // frontier.
@@ -25,16 +25,15 @@
 
 namespace gg {
 
-constexpr int32_t kChunk = 256;  // edges per queue entry
 constexpr int32_t kLanes = kBsLanes;
 constexpr int32_t kPrefetch = 8;  // distance lines in flight per warp
-// Queue entries active for at most this many sources are relaxed edge-parallel
-// (lanes = edges); busier ones source-parallel (lanes = sources).
-constexpr int32_t kEdgeParallelMax = 6;
+// Queue entries active for at most S.ep_max sources are relaxed edge-parallel
+// (lanes = edges); busier ones source-parallel (lanes = sources).  S.chunk
+// (edges per queue entry) and S.ep_max come from the graph's batch tuning.
 
 __device__ __forceinline__ void bs_enqueue(const BsState &S, int64_t *q, int32_t *qcnt, int32_t v) {
   const int32_t deg = S.off[v + 1] - S.off[v];
-  const int32_t nch = max(1, ceil_div(deg, kChunk));
+  const int32_t nch = max(1, ceil_div(deg, S.chunk));
   const int32_t pos = atomicAdd(qcnt, nch);
   if ((int64_t)pos + nch > S.qcap) {
     atomicOr(S.err, DEV_ERR_OVERFLOW);
@@ -73,16 +72,16 @@ __global__ void __launch_bounds__(256) k_bsssp(BsState S) {
       const int64_t *qi = S.q[in];
       int64_t *qo = S.q[in ^ 1];
       for (int64_t e = gwarp; e < n; e += nwarps) {
-        const int64_t item = qi[e];
+        const int64_t item = __ldcg(qi + e);
         const int32_t u = (int32_t)(item >> 32);
         const int32_t c = (int32_t)(item & 0xffffffff);
         const uint32_t m = __ldcg(S.fr + u);
         if (!m) continue;
         const bool act = (m >> lane) & 1u;
         const int32_t du = act ? __ldcg(S.dist + (int64_t)u * kLanes + lane) : INT_MAX;
-        const int32_t b = S.off[u] + c * kChunk;
-        const int32_t eend = min(b + kChunk, S.off[u + 1]);
-        if (__popc(m) <= kEdgeParallelMax) {
+        const int32_t b = S.off[u] + c * S.chunk;
+        const int32_t eend = min(b + S.chunk, S.off[u + 1]);
+        if (__popc(m) <= S.ep_max) {
           // Few active sources: lanes take edges, the warp loops over sources.
           uint32_t mm = m;
           while (mm) {
@@ -170,7 +169,7 @@ __global__ void __launch_bounds__(256) k_bsssp(BsState S) {
       for (int32_t e = tid; e < ceil_div(mq, tstride) * tstride; e += tstride) {
         uint32_t x = 0;
         if (e < mq) {
-          const int64_t item = qo[e];
+          const int64_t item = __ldcg(qo + e);
           if ((item & 0xffffffff) == 0) {
             const int32_t v = (int32_t)(item >> 32);
             x = __ldcg(S.nacc + v);
@@ -206,7 +205,7 @@ __global__ void __launch_bounds__(256) k_bsssp(BsState S) {
       // pass 1: per-source minimum far priority at or above the window
       int32_t mn = INT_MAX;
       for (int64_t e = gwarp; e < fcount; e += nwarps) {
-        const int32_t v = fla[e];
+        const int32_t v = __ldcg(fla + e);
         const uint32_t fm = __ldcg(S.far + v);
         if (adv_l && ((fm >> lane) & 1u)) {
           const int32_t d = __ldcg(S.dist + (int64_t)v * kLanes + lane);
@@ -227,7 +226,7 @@ __global__ void __launch_bounds__(256) k_bsssp(BsState S) {
       const int64_t hi = (int64_t)newcur + S.delta;
       int64_t *qo = S.q[in ^ 1];
       for (int64_t e = gwarp; e < fcount; e += nwarps) {
-        const int32_t v = fla[e];
+        const int32_t v = __ldcg(fla + e);
         const uint32_t fm = __ldcg(S.far + v);
         const bool f = (fm >> lane) & 1u;
         bool keep = false, move = false;
@@ -330,7 +329,7 @@ BsBuffers::~BsBuffers() {
 gg_status bsssp_buffers(gg_graph *g, int32_t nsrc, bool owned, BsBuffers *b) {
   const int32_t V = g->csr.V;
   const int64_t E = g->csr.E;
-  b->qcap = (int64_t)V + E / kChunk + 64;
+  b->qcap = (int64_t)V + E / kMinChunk + 64;  // any tuning's chunk fits
   b->owned = owned;
   const size_t sz[6] = {sizeof(int32_t) * (size_t)V * kLanes, sizeof(uint32_t) * 3 * (size_t)V,
                         sizeof(int32_t) * (3 * (size_t)V + 256), sizeof(int64_t) * 2 * (size_t)b->qcap,
@@ -371,12 +370,17 @@ BsState bsssp_state(gg_graph *g, const BsBuffers &b, int32_t delta) {
   S.w = g->csr.w;
   S.V = V;
   S.delta = delta;
+  const gg_batch_tuning t = effective_tuning(g, GG_BATCH_SSSP, 1);
+  S.chunk = t.chunk;
+  S.ep_max = t.edge_parallel_max;
   S.bar = g->d_bar;
   S.err = g->d_err;
   S.timeout_ns = barrier_timeout_ns();
   S.loop_limit_ns = loop_timeout_ns();
   return S;
 }
+
+const void *bsssp_kernel() { return (const void *)k_bsssp; }
 
 // One group of k <= 32 sources (device array dsrc): reset, seed, the
 // persistent loop, and the per-source rows into out_rows.  Issues only
@@ -395,7 +399,8 @@ gg_status bsssp_enqueue(gg_graph *g, cudaStream_t st, const BsState &S, const in
   void *args[] = {&arg};
   if (timed) GG_CUDA(cudaEventRecord(g->ev2, st));
   note_launch();
-  GG_CUDA(cudaLaunchCooperativeKernel((const void *)k_bsssp, per_sm * g->sm_count, 256, args, 0, st));
+  const int bps = effective_tuning(g, GG_BATCH_SSSP, per_sm).blocks_per_sm;
+  GG_CUDA(cudaLaunchCooperativeKernel((const void *)k_bsssp, bps * g->sm_count, 256, args, 0, st));
   if (timed) GG_CUDA(cudaEventRecord(g->ev3, st));
   note_launch();
   k_bsssp_out<<<g->sm_count * 8, 256, 0, st>>>(S.dist, S.V, k, out_rows);

@@ -44,7 +44,8 @@ struct Enum {
   __device__ __forceinline__ int32_t count() const {
     return n >= 0 ? n : *(volatile const int32_t *)n_dev;
   }
-  __device__ __forceinline__ int32_t at(int32_t i) const { return q ? __ldg(q + i) : i; }
+  // L2-coherent load: persistent kernels refill the queue they enumerate.
+  __device__ __forceinline__ int32_t at(int32_t i) const { return q ? __ldcg(q + i) : i; }
 };
 
 // Membership test against an input frontier (bitmap / boolmap), or "all".

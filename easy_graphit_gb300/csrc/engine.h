@@ -51,6 +51,7 @@ struct gg_graph {
   gg_frontier *app_frontier = nullptr;
   gg_pq *app_pq = nullptr;
   gg_frontier_list *app_list = nullptr;
+  gg_batch_tuning tuning[3] = {};  // batched BFS, SSSP, BC launch shapes (0 = default)
 };
 
 struct gg_frontier {
@@ -111,6 +112,9 @@ gg_status check_device_error(gg_graph *g, const char *what);
 gg_status scratch_get(gg_graph *g, int slot, size_t bytes, void **p);
 gg_status scratch_get_app(gg_graph *g, int slot, size_t bytes, void **p);
 int resident_grid(const void *kernel, int cta, size_t smem, int sm_count);
+
+// ---- pagerank.cu
+gg_status pagerank_pull_twc(gg_graph *g, int32_t iters, float damping, float *rank, float *contrib2);
 
 // ---- frontier.cu
 gg_status frontier_prepare_sparse(gg_frontier *f);

@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import ctypes as C
 from enum import IntEnum
+from pathlib import Path
 from typing import Optional
 
 import numpy as np
@@ -142,9 +143,26 @@ D, LB, FC, PR_ = (SimpleGPUSchedule.direction_type, SimpleGPUSchedule.load_balan
                   SimpleGPUSchedule.frontier_creation_type, SimpleGPUSchedule.pull_frontier_rep_type)
 
 
+class LearnedGPUSchedule:
+    """Per-iteration schedule from the learned selector; `fallback` (the
+    hand-written GraphIt schedule) is used when no selector is attached."""
+
+    def __init__(self, selector: "Selector", fallback: SimpleGPUSchedule | None = None):
+        self.selector = selector
+        self.fallback = fallback or SimpleGPUSchedule().configLoadBalancing(
+            SimpleGPUSchedule.load_balancing_type.TWCE)
+
+
 def app_schedule(s, fuse: bool = False) -> L.gg_app_schedule:
     a = L.gg_app_schedule()
     a.fuse = int(bool(fuse))
+    if isinstance(s, LearnedGPUSchedule):
+        a.kind = 2
+        a.s1 = s.fallback.to_c()
+        a.s2 = s.fallback.to_c()
+        a.selector = s.selector._h if s.selector is not None else None
+        a.fuse = 0
+        return a
     if isinstance(s, HybridGPUSchedule):
         a.kind = 1
         a.s1, a.s2, a.threshold = s.s1.to_c(), s.s2.to_c(), s.threshold
@@ -480,6 +498,17 @@ def bfs_batch(g: GraphT, sources, out=None):
     return out, _stats(st)
 
 
+def bc_batch(g: GraphT, sources, out=None):
+    """Batched BC (apps/bc.cpp per source, 64 sources per persistent launch).
+    Returns (dependencies [nsrc, V] float32, stats)."""
+    srcs = np.ascontiguousarray(sources, dtype=np.int32)
+    if out is None:
+        out = np.empty((len(srcs), g.num_vertices), dtype=np.float32)
+    st = L.gg_stats()
+    call("gg_bc_batch", g.handle, _np_ptr(srcs), len(srcs), _ptr(out), C.byref(st))
+    return out, _stats(st)
+
+
 def sssp_batch(g: GraphT, sources, delta: int, out=None):
     """Batched delta-stepping SSSP (32 sources per pass).  Returns
     (dist [nsrc, V] int32, stats)."""
@@ -492,14 +521,15 @@ def sssp_batch(g: GraphT, sources, delta: int, out=None):
 
 
 class BatchPlan:
-    """A batched BFS ("bfs") or SSSP ("sssp") captured into a CUDA graph once and
-    replayed by run().  `out` is a CUDA tensor of shape [nsrc, V] (int32)."""
+    """A batched BFS ("bfs"), SSSP ("sssp") or BC ("bc") captured into a CUDA
+    graph once and replayed by run().  `out` is a CUDA tensor of shape
+    [nsrc, V]: int32 for BFS and SSSP, float32 for BC."""
 
     def __init__(self, g: GraphT, app: str, sources, out, delta: int = 32):
         self.g = g
         srcs = np.ascontiguousarray(sources, dtype=np.int32)
         h = C.c_void_p()
-        call("gg_batch_plan_create", g.handle, {"bfs": 0, "sssp": 1}[app], _np_ptr(srcs), len(srcs),
+        call("gg_batch_plan_create", g.handle, BATCH_APPS[app], _np_ptr(srcs), len(srcs),
              delta, _ptr(out), C.byref(h))
         self._h = h
 
@@ -518,6 +548,34 @@ class BatchPlan:
             self.close()
         except Exception:
             pass
+
+
+BATCH_APPS = {"bfs": 0, "sssp": 1, "bc": 2}
+
+
+def set_batch_tuning(g: GraphT, app: str, blocks_per_sm: int = 0, chunk: int = 0,
+                     edge_parallel_max: int = 0) -> None:
+    """Launch shape of the graph's batched `app` kernels (0 = built-in default)."""
+    t = L.gg_batch_tuning(blocks_per_sm, chunk, edge_parallel_max)
+    call("gg_batch_set_tuning", g.handle, BATCH_APPS[app], C.byref(t))
+
+
+def get_batch_tuning(g: GraphT, app: str) -> dict:
+    t = L.gg_batch_tuning()
+    call("gg_batch_get_tuning", g.handle, BATCH_APPS[app], C.byref(t))
+    return t.as_dict()
+
+
+def autotune_batch(g: GraphT, app: str, sources, delta: int = 32, max_rows: int = 64):
+    """Runs the autotuner of the batched `app` on this graph; the winner becomes
+    the graph's tuning.  Returns (best tuning dict, [(tuning dict, ms), ...])."""
+    srcs = np.ascontiguousarray(sources, dtype=np.int32)
+    best = L.gg_batch_tuning()
+    rows = (L.gg_tune_row * max_rows)()
+    n = C.c_int32()
+    call("gg_batch_autotune", g.handle, BATCH_APPS[app], _np_ptr(srcs), len(srcs), delta,
+         C.byref(best), rows, max_rows, C.byref(n))
+    return best.as_dict(), [(rows[i].tuning.as_dict(), rows[i].ms) for i in range(min(n.value, max_rows))]
 
 
 def bfs_multi(g: GraphT, sources, schedule=None, fuse=None):
@@ -568,3 +626,104 @@ def bc(g: GraphT, src: int, schedule=None, fuse=None):
     a = _resolve("bc", schedule, fuse)
     call("gg_bc", g.handle, C.byref(a), src, _ptr(dep), C.byref(st))
     return dep, _stats(st)
+
+
+# --------------------------------------------------------- learned selector
+N_FEATURES, N_OUTPUTS, N_CANDIDATES = 12, 11, 36
+LB_HEAD = [SimpleGPUSchedule.load_balancing_type.TWCE, SimpleGPUSchedule.load_balancing_type.ETWC,
+           SimpleGPUSchedule.load_balancing_type.CM, SimpleGPUSchedule.load_balancing_type.WM,
+           SimpleGPUSchedule.load_balancing_type.VERTEX_BASED, SimpleGPUSchedule.load_balancing_type.EDGE_ONLY]
+SEL_APPS = {"bfs": 0, "sssp": 1, "cc": 2}
+
+
+def candidate_labels(c: int) -> tuple[int, int, int]:
+    """Candidate index -> (direction, load-balancing head index, frontier type)."""
+    return c // 18, (c // 3) % 6, c % 3
+
+
+class Selector:
+    """The bf16 MLP schedule selector (libgg.so kernels)."""
+
+    def __init__(self, seed: int = 1, _handle=None):
+        if _handle is None:
+            _handle = C.c_void_p()
+            call("gg_selector_create", seed, C.byref(_handle))
+        self._h = _handle
+
+    @classmethod
+    def load(cls, path: str) -> "Selector":
+        h = C.c_void_p()
+        call("gg_selector_load", str(path).encode(), C.byref(h))
+        return cls(_handle=h)
+
+    @classmethod
+    def pretrained(cls) -> "Selector":
+        """The model shipped with the package (selector_model.bin, trained by
+        easy_graphit_gb300.selector_train; its manifest is selector_model.json)."""
+        return cls.load(str(Path(__file__).resolve().parent / "selector_model.bin"))
+
+    def save(self, path: str) -> None:
+        call("gg_selector_save", self._h, str(path).encode())
+
+    @property
+    def params(self) -> np.ndarray:
+        n = lib().gg_selector_num_params()
+        out = np.empty(n, dtype=np.float32)
+        call("gg_selector_get_params", self._h, _np_ptr(out), n)
+        return out
+
+    @params.setter
+    def params(self, p) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        call("gg_selector_set_params", self._h, _np_ptr(p), len(p))
+
+    def forward(self, x) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        out = np.empty((len(x), N_OUTPUTS), dtype=np.float32)
+        call("gg_selector_forward", self._h, _np_ptr(x), len(x), _np_ptr(out))
+        return out
+
+    def grad(self, x, labels) -> tuple[np.ndarray, float]:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        labels = np.ascontiguousarray(labels, dtype=np.int32)
+        g = np.empty(lib().gg_selector_num_params(), dtype=np.float32)
+        loss = C.c_float()
+        call("gg_selector_grad", self._h, _np_ptr(x), _np_ptr(labels), len(x), _np_ptr(g), C.byref(loss))
+        return g, loss.value
+
+    def train(self, x, labels, epochs: int = 500, lr: float = 3e-3) -> float:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        labels = np.ascontiguousarray(labels, dtype=np.int32)
+        loss = C.c_float()
+        call("gg_selector_train", self._h, _np_ptr(x), _np_ptr(labels), len(x), epochs, lr, C.byref(loss))
+        return loss.value
+
+    def predict(self, x) -> np.ndarray:
+        z = self.forward(x)
+        return np.stack([z[:, 0:2].argmax(1), z[:, 2:8].argmax(1), z[:, 8:11].argmax(1)], axis=1)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gg_selector_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def collect_timings(g: GraphT, app: str, src: int = 0, delta: int = 32, max_rows: int = 4096):
+    """Per-iteration features [rows, 12] and candidate times [rows, 36] (ms)."""
+    feats = np.empty((max_rows, N_FEATURES), dtype=np.float32)
+    times = np.empty((max_rows, N_CANDIDATES), dtype=np.float32)
+    n = C.c_int32()
+    call("gg_selector_collect", g.handle, SEL_APPS[app], src, delta, max_rows, _np_ptr(feats),
+         _np_ptr(times), C.byref(n))
+    return feats[:n.value].copy(), times[:n.value].copy()
+
+
+def labels_from_times(times: np.ndarray) -> np.ndarray:
+    best = np.argmin(times, axis=1)
+    return np.array([candidate_labels(int(c)) for c in best], dtype=np.int32).reshape(-1, 3)

@@ -1,0 +1,154 @@
+"""Trains the learned schedule selector on timings generated by the engine.
+
+    python -m easy_graphit_gb300.selector_train [--out easy_graphit_gb300/selector_model.bin]
+
+Training graphs: R-MAT at scales 18 to 24 with skew a in [0.45, 0.75] (b = c =
+(0.95 - a) / 2) and 2-D grids, GAPBS-seeded; for each, BFS and SSSP runs
+(delta 32) and CC.  At every iteration the engine times all 36 candidate
+schedules on the same state (gg_selector_collect); the fastest candidate's
+(direction, load balancing, frontier type) is the label.  Training is
+full-batch Adam on the GPU kernels.  Evaluation uses held-out seeds: the
+learned schedule against the apps' hand-written GraphIt schedules, results
+checked bit-exact against the oracle.  Writes the parameter file and a JSON
+manifest beside it.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+from pathlib import Path
+
+import numpy as np
+
+from .graphit import (GraphT, HostGraph, LearnedGPUSchedule, Selector, bfs, cc, collect_timings,
+                      default_schedule, labels_from_times, sssp)
+
+PKG = Path(__file__).resolve().parent
+DEFAULT_OUT = PKG / "selector_model.bin"
+
+TRAIN_SEEDS = [101, 102, 103]
+HELDOUT_SEEDS = [901, 902]
+
+
+def rmat(scale, a, seed, sym):
+    b = (0.95 - a) / 2
+    return HostGraph.rmat(scale, 16, a=a, b=b, c=b, seed=seed, symmetrize=sym)
+
+
+def training_graphs(scales, skews):
+    out = []
+    for i, scale in enumerate(scales):
+        for j, a in enumerate(skews):
+            out.append((f"rmat{scale}_a{a:.2f}", scale, a, TRAIN_SEEDS[(i + j) % len(TRAIN_SEEDS)]))
+    return out
+
+
+def collect(scales, skews, grids, max_rows, log):
+    X, T = [], []
+    for name, scale, a, seed in training_graphs(scales, skews):
+        for app in ("bfs", "cc", "sssp"):
+            sym = app != "sssp"
+            hg = rmat(scale, a, seed, sym)
+            g = GraphT(hg, symmetric=sym)
+            srcs = hg.pick_sources(2 if app == "bfs" else 1, seed=seed)
+            for s in srcs:
+                t0 = time.time()
+                f, t = collect_timings(g, app, int(s), 32, max_rows)
+                X.append(f)
+                T.append(t)
+                log(f"{name} {app} src={int(s)} rows={len(f)} ({time.time() - t0:.1f}s)")
+                if app == "cc":
+                    break
+            g.close()
+    for n in grids:
+        hg = HostGraph.grid(n, n, seed=TRAIN_SEEDS[0])
+        g = GraphT(hg, symmetric=True)
+        for app in ("bfs", "sssp"):
+            s = int(hg.pick_sources(1, seed=7)[0])
+            f, t = collect_timings(g, app, s, 32, max_rows)
+            X.append(f)
+            T.append(t)
+            log(f"grid{n} {app} rows={len(f)}")
+        g.close()
+    return np.concatenate(X), np.concatenate(T)
+
+
+def evaluate(model, scale, log):
+    """Held-out graphs: learned schedule vs the apps' hand-written schedules;
+    both must produce identical results."""
+    rows = []
+    for seed in HELDOUT_SEEDS:
+        for app in ("bfs", "sssp", "cc"):
+            sym = app != "sssp"
+            hg = rmat(scale, 0.57, seed, sym)
+            g = GraphT(hg, symmetric=sym)
+            src = int(hg.pick_sources(1, seed=seed)[0])
+            plain, fuse = default_schedule(app)
+            learned = LearnedGPUSchedule(model)
+            times, outs = {}, {}
+            for label, sch, fz in (("plain", plain, fuse), ("learned", learned, False)):
+                best = None
+                for _ in range(3):
+                    if app == "bfs":
+                        out, _, st = bfs(g, src, sch, fz)
+                    elif app == "sssp":
+                        out, st = sssp(g, src, 32, sch, fz)
+                    else:
+                        out, st = cc(g, sch)
+                    outs[label] = out
+                    best = st["device_ms"] if best is None else min(best, st["device_ms"])
+                times[label] = best
+            if not np.array_equal(outs["plain"], outs["learned"]):
+                raise AssertionError(f"{app}: learned and plain schedules disagree")
+            rows.append({"app": app, "seed": seed, "scale": scale, "plain_ms": times["plain"],
+                         "learned_ms": times["learned"], "speedup": times["plain"] / times["learned"]})
+            log(f"heldout {app} seed={seed}: plain {times['plain']:.2f} ms, learned {times['learned']:.2f} ms")
+            g.close()
+    return rows
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--out", default=str(DEFAULT_OUT))
+    p.add_argument("--scales", default="18,20,22,24")
+    p.add_argument("--skews", default="0.45,0.57,0.75")
+    p.add_argument("--grids", default="256,512")
+    p.add_argument("--max-rows", type=int, default=120)
+    p.add_argument("--epochs", type=int, default=3000)
+    p.add_argument("--lr", type=float, default=3e-3)
+    p.add_argument("--eval-scale", type=int, default=20)
+    a = p.parse_args()
+    log = lambda m: print(m, flush=True)
+    scales = [int(s) for s in a.scales.split(",")]
+    skews = [float(s) for s in a.skews.split(",")]
+    grids = [int(s) for s in a.grids.split(",") if s]
+    t0 = time.time()
+    X, T = collect(scales, skews, grids, a.max_rows, log)
+    lab = labels_from_times(T)
+    log(f"collected {len(X)} rows in {time.time() - t0:.1f}s")
+    model = Selector(seed=27491095)
+    loss = model.train(X, lab, epochs=a.epochs, lr=a.lr)
+    acc = (model.predict(X) == lab).mean(0)
+    # time of the predicted candidate relative to the fastest, per row
+    pred = model.predict(X)
+    cand = pred[:, 0] * 18 + pred[:, 1] * 3 + pred[:, 2]
+    regret = float(np.mean(T[np.arange(len(T)), cand] / T.min(1)))
+    log(f"loss {loss:.4f} accuracy {acc} mean time / best {regret:.3f}")
+    model.save(a.out)
+    evals = evaluate(model, a.eval_scale, log)
+    manifest = {
+        "file": Path(a.out).name, "params": int(len(model.params)),
+        "architecture": "12 -> 64 -> 64 -> 11 (bf16 MLP; heads: direction 2, load balancing 6, frontier 3)",
+        "training": {"rows": int(len(X)), "scales": scales, "skews": skews, "grids": grids,
+                     "seeds": TRAIN_SEEDS, "apps": ["bfs", "sssp (delta 32)", "cc"],
+                     "epochs": a.epochs, "lr": a.lr, "final_loss": loss,
+                     "accuracy": [float(v) for v in acc], "mean_time_over_best": regret},
+        "heldout": evals,
+    }
+    Path(a.out).with_suffix(".json").write_text(json.dumps(manifest, indent=1))
+    log(json.dumps(manifest))
+
+
+if __name__ == "__main__":
+    main()

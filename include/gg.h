@@ -318,6 +318,43 @@ gg_status gg_cc(gg_graph *g, const gg_app_schedule *s, int32_t *labels_out,
 gg_status gg_bc(gg_graph *g, const gg_app_schedule *s, int32_t src,
                 float *dep_out, gg_stats *stats);
 
+/* ------------------------------------------------- learned schedule selector
+ * No reference counterpart.  A bf16 MLP (12 features -> 64 -> 64 -> 11 logits)
+ * whose heads choose, per iteration, the direction (push/pull), the load
+ * balancing (TWCE, ETWC, CM, WM, VERTEX_BASED, EDGE_ONLY) and the output frontier type
+ * (queue, bitmap, boolmap).  Forward and backward are hand-written tensor-core
+ * kernels (mma.sync bf16, fp32 accumulation); training is full-batch Adam on
+ * fp32 master weights.  Used by app schedules of kind GG_SCHED_LEARNED, whose
+ * s1 is the fallback when no selector is attached.
+ * Features (per iteration): log2 of frontier vertices, frontier edges,
+ * unvisited vertices and edges, frontier degree mean/max/variance; iteration
+ * index; log2 V and E; frontier share of V and of E.
+ * Labels: int32 triples (direction 0..1, load balancing 0..5, frontier 0..2). */
+enum { GG_SEL_BFS = 0, GG_SEL_SSSP = 1, GG_SEL_CC = 2 };
+typedef struct gg_selector gg_selector;
+gg_status gg_selector_create(int64_t seed, gg_selector **out);
+gg_status gg_selector_destroy(gg_selector *s);
+int32_t gg_selector_num_params(void);
+gg_status gg_selector_get_params(const gg_selector *s, float *out, int32_t n);
+gg_status gg_selector_set_params(gg_selector *s, const float *in, int32_t n);
+/* logits[n][11] of features x[n][12] (host or device memory). */
+gg_status gg_selector_forward(gg_selector *s, const float *x, int32_t n, float *logits);
+/* Gradient (all parameters) and loss of the mean summed cross-entropy. */
+gg_status gg_selector_grad(gg_selector *s, const float *x, const int32_t *labels,
+                           int32_t n, float *grad, float *loss);
+gg_status gg_selector_train(gg_selector *s, const float *x, const int32_t *labels,
+                            int32_t n, int32_t epochs, float lr, float *final_loss);
+gg_status gg_selector_save(const gg_selector *s, const char *path);
+gg_status gg_selector_load(const char *path, gg_selector **out);
+/* Training data generated by the engine: runs `app` from src (delta for SSSP)
+ * with the fallback schedule and, at each iteration, times all 36 candidate
+ * schedules (candidate c = direction*18 + lb*3 + frontier) on the same state.
+ * feats[max_rows][12], times[max_rows][36] in ms (INFINITY if a candidate
+ * failed); *nrows = iterations recorded. */
+gg_status gg_selector_collect(gg_graph *g, int32_t app, int32_t src, int32_t delta,
+                              int32_t max_rows, float *feats, float *times,
+                              int32_t *nrows);
+
 /* ----------------------------------------------------- allocation-free BFS
  * No counterpart in the reference: an extra entry point for callers that may
  * not allocate device memory while they run (code inside someone else's
@@ -345,20 +382,59 @@ gg_status gg_bfs_noalloc(const int32_t *offsets, const int32_t *dst,
  *    depth_out[s*V + v] (host or device memory, nsrc*V int32).
  *  gg_sssp_batch: 32 sources per pass with per-source delta-stepping windows
  *    (gpu_priority_queue.h semantics) and a far pile instead of O(V) bucket
- *    scans; dist_out[s*V + v] (INT_MAX unreached). */
+ *    scans; dist_out[s*V + v] (INT_MAX unreached).
+ *  gg_bc_batch: BC dependencies of apps/bc.cpp for 64 sources per pass (the
+ *    levels of one bit-parallel BFS shared by all sources; sigma and
+ *    dependencies gathered per source in fp64); dep_out[s*V + v] (fp32, host
+ *    or device memory, 0 where unreached).  Needs 64*V < 2^31.
+ *    stats->edges_traversed = 2 * sum over sources of the reached out-edges. */
 gg_status gg_bfs_batch(gg_graph *g, const int32_t *sources, int32_t nsrc,
                        int32_t *depth_out, gg_stats *stats);
-/* Batch plans: a whole gg_bfs_batch / gg_sssp_batch captured once into a CUDA
- * graph (every persistent launch of every group of sources) and replayed with
- * one graph launch per run.  `out` must be device memory (nsrc*V int32); the
- * plan copies the sources and owns its device state. */
+gg_status gg_bc_batch(gg_graph *g, const int32_t *sources, int32_t nsrc,
+                      float *dep_out, gg_stats *stats);
+/* Batch plans: a whole gg_bfs_batch / gg_sssp_batch / gg_bc_batch captured
+ * once into a CUDA graph (every persistent launch of every group of sources)
+ * and replayed with one graph launch per run.  `out` must be device memory:
+ * nsrc*V int32 (BFS depths, SSSP distances) or float (BC dependencies).  The
+ * plan copies the sources and owns its device state; delta is used by SSSP. */
 typedef struct gg_batch_plan gg_batch_plan;
-enum { GG_BATCH_BFS = 0, GG_BATCH_SSSP = 1 };
+enum { GG_BATCH_BFS = 0, GG_BATCH_SSSP = 1, GG_BATCH_BC = 2 };
 gg_status gg_batch_plan_create(gg_graph *g, int32_t app, const int32_t *sources,
-                               int32_t nsrc, int32_t delta, int32_t *out,
+                               int32_t nsrc, int32_t delta, void *out,
                                gg_batch_plan **plan);
 gg_status gg_batch_plan_run(gg_batch_plan *plan, gg_stats *stats);
 gg_status gg_batch_plan_destroy(gg_batch_plan *plan);
+/* Launch shape of a graph's batched kernels (no reference counterpart).
+ * Zero fields take the built-in default.  Results never depend on it.
+ *  blocks_per_sm      persistent CTAs per SM, capped at what fits (default:
+ *                     all that fit);
+ *  chunk              edges per work item of batched SSSP and BC, a power of
+ *                     two in [32, 4096] (default 256);
+ *  edge_parallel_max  batched SSSP: work items active for at most this many
+ *                     sources map lanes to edges, the others lanes to sources
+ *                     (default 6; -1 = never edge-parallel; at most 32).
+ * The tuning of `app` (GG_BATCH_*) applies to the batched calls and to plans
+ * created after it is set. */
+typedef struct gg_batch_tuning {
+  int32_t blocks_per_sm;
+  int32_t chunk;
+  int32_t edge_parallel_max;
+} gg_batch_tuning;
+gg_status gg_batch_set_tuning(gg_graph *g, int32_t app, const gg_batch_tuning *t);
+gg_status gg_batch_get_tuning(const gg_graph *g, int32_t app, gg_batch_tuning *t);
+/* Autotuner: times candidate launch shapes of `app` on the graph (one pass
+ * over the first min(nsrc, pass width) sources per candidate, best of two
+ * timed runs of the persistent kernel), by coordinate descent over
+ * blocks_per_sm, then chunk, then edge_parallel_max; sets the fastest as the
+ * graph's tuning and returns it in *best.  Every trial goes to rows (at most
+ * max_rows; *nrows = trials run).  delta is used by SSSP. */
+typedef struct gg_tune_row {
+  gg_batch_tuning tuning;
+  float ms;
+} gg_tune_row;
+gg_status gg_batch_autotune(gg_graph *g, int32_t app, const int32_t *sources,
+                            int32_t nsrc, int32_t delta, gg_batch_tuning *best,
+                            gg_tune_row *rows, int32_t max_rows, int32_t *nrows);
 /* Multi-source traversal with the app schedule: every source starts at 0 and
  * out[v] is the distance to the nearest source.  With one source per part of a
  * gg_host_graph_union this runs many graphs of uneven size in one persistent

@@ -186,13 +186,28 @@ def test_sssp_grid_and_power_schedule():
     sched(direction=T.direction_type.PULL, lb=T.load_balancing_type.VERTEX_BASED),
     sched(direction=T.direction_type.PUSH, lb=T.load_balancing_type.TWCE),
     sched(direction=T.direction_type.PULL, lb=T.load_balancing_type.CM),
+    sched(direction=T.direction_type.PULL, lb=T.load_balancing_type.TWC),
 ], ids=["default", "pull_edge_only", "push_edge_only_blocked", "pull_wm", "pull_vertex",
-        "push_twce", "pull_cm"])
+        "push_twce", "pull_cm", "pull_twc_static"])
 def test_pagerank(sc):
     hg, g, (off, dst, _) = graph("dir16")
     ref = oracle.pagerank(off, dst, 20, float(np.float32(0.85)))
     r, st = pagerank(g, 20, 0.85, None if sc == "default" else sc)
     assert rel_l1(r, ref) <= PR_TOL, rel_l1(r, ref)
+
+
+@pytest.mark.parametrize("kind", ["sym16", "dir16"])
+def test_pagerank_static_pull_is_bitwise_deterministic(kind):
+    """PULL + TWC runs the static pull gather: one owner per vertex, fixed
+    summation order, so two runs agree bit for bit."""
+    hg, g, (off, dst, _) = graph(kind)
+    sc = sched(direction=T.direction_type.PULL, lb=T.load_balancing_type.TWC)
+    ref = oracle.pagerank(off, dst, 20, float(np.float32(0.85)))
+    r1, st = pagerank(g, 20, 0.85, sc)
+    r2, _ = pagerank(g, 20, 0.85, sc)
+    np.testing.assert_array_equal(r1, r2)
+    assert rel_l1(r1, ref) <= PR_TOL, rel_l1(r1, ref)
+    assert st["iterations"] == 20 and st["edges_traversed"] == 20 * len(dst)
 
 
 # --------------------------------------------------------------------- CC

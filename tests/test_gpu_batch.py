@@ -124,3 +124,123 @@ def test_batch_plan_cuda_graph_replay(app):
             np.testing.assert_array_equal(got[i], ref)
         out.fill_(-7)
     plan.close()
+
+
+# ---------------------------------------------------------------- batched BC
+BC_TOL = 1e-6  # relative L1 against the FP64 oracle, per source
+
+
+@pytest.mark.parametrize("kind", ["sym14", "dir14", "grid"])
+@pytest.mark.parametrize("nsrc", [1, 17, 64, 70])
+def test_bc_batch_matches_fp64_oracle(kind, nsrc):
+    from easy_graphit_gb300 import bc_batch
+    from tests.conftest import rel_l1
+    hg, g, (off, dst, _) = graph(kind)
+    srcs = hg.pick_sources(nsrc, seed=13)
+    dep, st = bc_batch(g, srcs)
+    assert dep.dtype == np.float32 and dep.shape == (nsrc, hg.num_vertices)
+    er = 0
+    for i, s in enumerate(srcs):
+        ref = oracle.bc(off, dst, int(s))
+        assert rel_l1(dep[i], ref) <= BC_TOL, (i, rel_l1(dep[i], ref))
+        er += oracle.reached_edges(off, oracle.bfs(off, dst, int(s)))
+    assert st["edges_traversed"] == 2 * er
+
+
+def test_bc_batch_equals_single_source_app():
+    from easy_graphit_gb300 import bc, bc_batch
+    from tests.conftest import rel_l1
+    hg, g, (off, dst, _) = graph("sym14")
+    srcs = hg.pick_sources(9, seed=21)
+    dep, _ = bc_batch(g, srcs)
+    for i, s in enumerate(srcs):
+        one, _ = bc(g, int(s))
+        assert rel_l1(dep[i], one) <= BC_TOL
+
+
+def test_bc_batch_duplicate_and_isolated_sources():
+    from easy_graphit_gb300 import bc_batch
+    from tests.conftest import rel_l1
+    # vertex 5 has no edges: its row is all zeros
+    edges = [(0, 1), (1, 2), (2, 3), (3, 0), (1, 3), (4, 0)]
+    src = [a for a, b in edges] + [b for a, b in edges]
+    dst_ = [b for a, b in edges] + [a for a, b in edges]
+    hg = HostGraph.from_edges(6, src, dst_, [1] * len(src))
+    g = GraphT(hg, symmetric=True)
+    off, dst = np.array(hg.offsets), np.array(hg.dst)
+    dep, _ = bc_batch(g, [1, 1, 5, 0])
+    for i, s in enumerate([1, 1, 5, 0]):
+        ref = oracle.bc(off, dst, s)
+        assert rel_l1(dep[i], ref) <= BC_TOL, (s, dep[i], ref)
+    assert not dep[2].any()
+
+
+def test_batch_plan_bc_replay():
+    import torch
+    from easy_graphit_gb300 import BatchPlan
+    from tests.conftest import rel_l1
+    hg, g, (off, dst, _) = graph("sym14")
+    srcs = hg.pick_sources(66, seed=4)
+    out = torch.full((66, hg.num_vertices), -7.0, dtype=torch.float32, device="cuda")
+    plan = BatchPlan(g, "bc", srcs, out)
+    for _ in range(2):
+        st = plan.run()
+        got = out.cpu().numpy()
+        for i in [0, 40, 63, 64, 65]:
+            assert rel_l1(got[i], oracle.bc(off, dst, int(srcs[i]))) <= BC_TOL
+        assert st["edges_traversed"] > 0
+        out.fill_(-7.0)
+    plan.close()
+
+
+# ------------------------------------------------------------- launch tuning
+@pytest.mark.parametrize("tuning", [dict(blocks_per_sm=1), dict(chunk=32), dict(chunk=4096),
+                                    dict(edge_parallel_max=-1), dict(edge_parallel_max=32),
+                                    dict(blocks_per_sm=2, chunk=64, edge_parallel_max=2)])
+def test_batched_results_do_not_depend_on_tuning(tuning):
+    from easy_graphit_gb300 import bc_batch, set_batch_tuning
+    from tests.conftest import rel_l1
+    hg, g, (off, dst, w) = graph("dir14")
+    srcs = hg.pick_sources(33, seed=17)
+    for app in ("bfs", "sssp", "bc"):
+        set_batch_tuning(g, app, **tuning)
+    try:
+        dist, _ = sssp_batch(g, srcs, 8)
+        depth, _ = bfs_batch(g, srcs)
+        dep, _ = bc_batch(g, srcs[:5])
+        for i in [0, 16, 32]:
+            s = int(srcs[i])
+            np.testing.assert_array_equal(dist[i], oracle.sssp_dijkstra(off, dst, w, s))
+            np.testing.assert_array_equal(depth[i], oracle.bfs(off, dst, s))
+        for i in range(5):
+            assert rel_l1(dep[i], oracle.bc(off, dst, int(srcs[i]))) <= BC_TOL
+    finally:
+        for app in ("bfs", "sssp", "bc"):
+            set_batch_tuning(g, app)
+
+
+def test_invalid_tuning_is_rejected():
+    from easy_graphit_gb300 import set_batch_tuning
+    hg, g, _ = graph("dir14")
+    for bad in (dict(chunk=48), dict(chunk=16), dict(chunk=8192), dict(edge_parallel_max=33),
+                dict(blocks_per_sm=-1)):
+        with pytest.raises(Exception, match="out of range"):
+            set_batch_tuning(g, "sssp", **bad)
+
+
+@pytest.mark.parametrize("app", ["bfs", "sssp", "bc"])
+def test_autotune_sets_the_fastest_candidate(app):
+    from easy_graphit_gb300 import autotune_batch, get_batch_tuning, set_batch_tuning
+    hg, g, (off, dst, w) = graph("sym14")
+    srcs = hg.pick_sources(32, seed=2)
+    best, rows = autotune_batch(g, app, srcs, delta=32)
+    try:
+        assert len(rows) >= 2 and all(ms > 0 for _, ms in rows)
+        assert min(rows, key=lambda r: r[1])[0] == best
+        assert get_batch_tuning(g, app) == best
+        if app == "sssp":  # the tuned graph still gives exact results
+            dist, _ = sssp_batch(g, srcs[:3], 32)
+            for i in range(3):
+                np.testing.assert_array_equal(dist[i], oracle.sssp_dijkstra(off, dst, w, int(srcs[i])))
+    finally:
+        set_batch_tuning(g, app)
