@@ -51,6 +51,10 @@ def parse():
     p.add_argument("--delta", type=int, default=32,
                    help="delta-stepping bucket width (both arms); 0 = autotune over {1,8,32,128}")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--tuning", choices=["auto", "default"], default="auto",
+                   help="launch shape of the batched kernels: autotuned on the graph, or the built-in one")
+    p.add_argument("--no-apps", action="store_true",
+                   help="omit the per-app comparison lines (BFS, BC, PageRank)")
     return p.parse_args()
 
 
@@ -206,7 +210,8 @@ def run_gb300(args):
     import torch
     import torch.distributed as dist
 
-    from easy_graphit_gb300 import GraphT, _lib as L, app_schedule, default_schedule
+    from easy_graphit_gb300 import (GraphT, LearnedGPUSchedule, Selector, _lib as L, app_schedule,
+                                    autotune_batch, default_schedule)
     from easy_graphit_gb300 import SimpleGPUSchedule as T
     from easy_graphit_gb300.replicas import aggregate_teps, rank_sources
 
@@ -247,6 +252,12 @@ def run_gb300(args):
                 best = (t, d)
         delta = best[1]
 
+    # Launch shape of the batched kernel (CTAs per SM, edges per queue entry,
+    # edge-parallel threshold), autotuned on this graph; untimed.
+    tuned, tune_rows = None, []
+    if args.tuning == "auto":
+        tuned, tune_rows = autotune_batch(g, "sssp", h_src, delta)
+
     # Algorithmic work per source (untimed): E_r, V_r from the distances.
     batched(delta, base)
     dd = dist_dev.cpu().numpy()
@@ -273,6 +284,7 @@ def run_gb300(args):
     twce = T()
     twce.configLoadBalancing(T.load_balancing_type.TWCE)
     twce_gteps = single(twce, True)
+    learned_gteps = single(LearnedGPUSchedule(Selector.pretrained()), False)
     batched(delta, base)
     assert np.array_equal(dist_dev.cpu().numpy(), dd), "batched and single-source distances differ"
 
@@ -319,6 +331,8 @@ def run_gb300(args):
     assert np.array_equal(h_out.numpy(), dd)
     e2e_val, e2e_ms = aggregate_teps(total_edges, e2e_ms, device=dev)
 
+    apps = None if args.no_apps else per_app(g, hg, off, dst, dev, stream)
+
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -344,6 +358,11 @@ def run_gb300(args):
                    "plain_gteps": plain_gteps,
                    "plain_schedule": "PUSH SPARSE VERTEX_BASED fused, one source at a time (sssp.cpp default)",
                    "single_twce_gteps": twce_gteps,
+                   "single_learned_gteps": learned_gteps,
+                   "learned_schedule": "LearnedGPUSchedule(Selector.pretrained()), unfused, one source at a time",
+                   "batch_tuning": tuned if tuned else "built-in (blocks_per_sm all that fit, chunk 256, "
+                                                        "edge_parallel_max 6)",
+                   "autotune_trials": len(tune_rows),
                    "batched_over_plain": value / world / plain_gteps,
                    "l2": "inputs larger than L2 (CSR %.2f GB, distances %.2f GB)"
                    % ((off.nbytes + dst.nbytes + w.nbytes) / 1e9, N_SOURCES * V * 4 / 1e9),
@@ -357,10 +376,66 @@ def run_gb300(args):
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
         "clocks": clk.summary(),
         "gpu_launches": launches,
+        "apps": apps,
     }
     print(json.dumps(out))
     if world > 1:
         dist.destroy_process_group()
+
+
+def per_app(g, hg, off, dst, dev, stream):
+    """Plain (the app's own schedule, one source at a time) against the batched
+    or static-gather path on the same graph, device-timed; outputs compared."""
+    import torch
+
+    from easy_graphit_gb300 import (SimpleGPUSchedule as T, bc, bc_batch, bfs, bfs_batch,
+                                    default_schedule, pagerank)
+    E = hg.num_edges
+    srcs = np.ascontiguousarray(hg.pick_sources(64, seed=27491095), dtype=np.int32)
+    res = {}
+    # BFS: bfs.cpp's PUSH TWCE fused per source vs 64 sources per launch
+    sch, fz = default_schedule("bfs")
+    t_plain, er, rows = 0.0, 0, []
+    for s in srcs:
+        d, _, st = bfs(g, int(s), sch, fz)
+        t_plain += st["device_ms"]
+        er += int(np.diff(off)[d >= 0].sum())
+        rows.append(d)
+    bfs_batch(g, srcs)
+    depth, st = bfs_batch(g, srcs)
+    res["bfs"] = {"sources": len(srcs), "plain_gteps": er / t_plain / 1e6,
+                  "batched_gteps": er / st["loop_ms"] / 1e6,
+                  "exact": bool(np.array_equal(depth, np.stack(rows))),
+                  "plain_schedule": "PUSH TWCE fused (bfs.cpp default)"}
+    # BC: bc.cpp's PUSH TWCE fused per source vs 64 sources per launch
+    sch, fz = default_schedule("bc")
+    t_plain, er2, rows = 0.0, 0, []
+    for s in srcs:
+        dep, st = bc(g, int(s), sch, fz)
+        t_plain += st["device_ms"]
+        er2 += st["edges_traversed"]
+        rows.append(dep)
+    bc_batch(g, srcs)
+    dep_b, st = bc_batch(g, srcs)
+    ref = np.stack(rows).astype(np.float64)
+    rel = float(np.abs(dep_b - ref).sum() / max(np.abs(ref).sum(), 1e-300))
+    res["bc"] = {"sources": len(srcs), "plain_gteps": er2 / t_plain / 1e6,
+                 "batched_gteps": st["edges_traversed"] / st["loop_ms"] / 1e6,
+                 "rel_l1_batched_vs_plain": rel,
+                 "plain_schedule": "PUSH TWCE fused (bc.cpp default); TEPS = 2 E_r / t"}
+    # PageRank: pr.cpp's PULL EDGE_ONLY blocked vs PULL TWC (static in-degree bins)
+    sch, _ = default_schedule("pr")
+    pagerank(g, 20, 0.85, sch)
+    r_plain, st_p = pagerank(g, 20, 0.85, sch)
+    tw = T().configDirection(T.direction_type.PULL).configLoadBalancing(T.load_balancing_type.TWC)
+    pagerank(g, 20, 0.85, tw)
+    r_tw, st_t = pagerank(g, 20, 0.85, tw)
+    res["pr"] = {"iterations": 20, "plain_gteps": 20 * E / st_p["device_ms"] / 1e6,
+                 "static_pull_gteps": 20 * E / st_t["device_ms"] / 1e6,
+                 "rel_l1_static_vs_plain": float(np.abs(r_tw.astype(np.float64) - r_plain).sum()
+                                                 / np.abs(r_plain.astype(np.float64)).sum()),
+                 "plain_schedule": "PULL EDGE_ONLY blocked 0x42000 (pr.cpp default)"}
+    return res
 
 
 def main():

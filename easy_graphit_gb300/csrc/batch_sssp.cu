@@ -31,6 +31,8 @@ constexpr int32_t kPrefetch = 8;  // distance lines in flight per warp
 // (lanes = edges); busier ones source-parallel (lanes = sources).  S.chunk
 // (edges per queue entry) and S.ep_max come from the graph's batch tuning.
 
+constexpr uint32_t kFull = 0xffffffffu;
+
 __device__ __forceinline__ void bs_enqueue(const BsState &S, int64_t *q, int32_t *qcnt, int32_t v) {
   const int32_t deg = S.off[v + 1] - S.off[v];
   const int32_t nch = max(1, ceil_div(deg, S.chunk));
@@ -42,8 +44,161 @@ __device__ __forceinline__ void bs_enqueue(const BsState &S, int64_t *q, int32_t
   for (int32_t c = 0; c < nch; ++c) q[pos + c] = ((int64_t)v << 32) | (uint32_t)c;
 }
 
-__global__ void __launch_bounds__(256) k_bsssp(BsState S) {
+// Entries per warp step: 32 when the list is long, fewer when it is short.
+__device__ __forceinline__ int32_t bs_batch(int64_t n, int64_t nwarps) {
+  const int64_t per = (n + nwarps - 1) / nwarps;
+  return (int32_t)(per < 1 ? 1 : (per > 32 ? 32 : per));
+}
+
+__device__ __forceinline__ void bs_far_push(const BsState &S, int p, int32_t v) {
+  const int32_t pos = atomicAdd(S.cnt + 3 + p, 1);
+  if (pos < S.V)
+    S.fl[p][pos] = v;
+  else
+    atomicOr(S.err, DEV_ERR_OVERFLOW);
+}
+
+// Relax of queue entries by warps, which take batches of up to 32 entries from
+// a shared counter (guided: batches shrink as the queue drains, so the phase
+// ends evenly): lane l loads entry l's vertex, frontier mask and edge range, so
+// the per-entry load chains overlap.  Entries active for at most ep_max sources have their edges
+// flattened over the lanes (lane = edge, looping over the entry's sources);
+// the others run one at a time with lane = source.
+__device__ __forceinline__ void bs_relax(const BsState &S, int64_t n, const int64_t *qi, int64_t *qo,
+                                         int32_t *qcnt_out, int32_t cut, const int32_t *s_cut, int p,
+                                         int32_t it, int32_t *wctr, int64_t nwarps) {
+  const int32_t lane = threadIdx.x & 31;
+  for (;;) {
+    int32_t e0 = 0, B = 1;
+    if (lane == 0) {
+      const int64_t left = n - *(volatile int32_t *)wctr;
+      B = bs_batch(left > 0 ? left / 2 : 1, nwarps);
+      e0 = atomicAdd(wctr, B);
+    }
+    e0 = __shfl_sync(kFull, e0, 0);
+    B = __shfl_sync(kFull, B, 0);
+    if (e0 >= n) break;
+    const int64_t e = (int64_t)e0 + lane;
+    int32_t u = 0, b = 0, cnt = 0;
+    uint32_t m = 0;
+    if (lane < B && e < n) {
+      const int64_t item = __ldcg(qi + e);
+      u = (int32_t)(item >> 32);
+      const int32_t c = (int32_t)(item & 0xffffffff);
+      m = __ldcg(S.fr + u);
+      if (m) {
+        const int32_t o1 = __ldg(S.off + u + 1);
+        b = __ldg(S.off + u) + c * S.chunk;
+        cnt = max(0, min(b + S.chunk, o1) - b);
+      }
+    }
+    const bool sparse = __popc(m) <= S.ep_max;
+    // (a) sparsely-active entries: lane = edge of the flattened edge list
+    {
+      const int32_t sc = sparse ? cnt : 0;
+      int32_t incl = sc;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int32_t t = __shfl_up_sync(kFull, incl, d);
+        if (lane >= d) incl += t;
+      }
+      const int32_t total = __shfl_sync(kFull, incl, 31);
+      const int32_t excl = incl - sc;
+      for (int32_t t0 = 0; t0 < total; t0 += 32) {
+        const int32_t idx = t0 + lane;
+        int32_t j = 0;  // the last entry whose exclusive offset is <= idx
+#pragma unroll
+        for (int st = 16; st > 0; st >>= 1) {
+          const int32_t ex = __shfl_sync(kFull, excl, j + st);
+          if (ex <= idx) j += st;
+        }
+        const int32_t uj = __shfl_sync(kFull, u, j);
+        const int32_t bj = __shfl_sync(kFull, b, j);
+        const int32_t exj = __shfl_sync(kFull, excl, j);
+        const uint32_t mj = __shfl_sync(kFull, m, j);
+        if (idx < total) {
+          const int32_t k = bj + (idx - exj);
+          const int32_t v = __ldg(S.dst + k), w = __ldg(S.w + k);
+          uint32_t mm = mj;
+          while (mm) {
+            const int32_t s = __ffs(mm) - 1;
+            mm &= mm - 1;
+            const int32_t du = __ldcg(S.dist + (int64_t)uj * kLanes + s);
+            if (du == INT_MAX) continue;
+            const int32_t np = du + w;
+            int32_t *pd = S.dist + (int64_t)v * kLanes + s;
+            if (np < __ldcg(pd) && atomicMin(pd, np) > np) {
+              if (np < s_cut[s]) {
+                atomicOr(S.nacc + v, 1u << s);
+                if (atomicMax(S.qstamp + v, it) < it) bs_enqueue(S, qo, qcnt_out, v);
+              } else if (atomicOr(S.far + v, 1u << s) == 0u) {
+                bs_far_push(S, p, v);
+              }
+            }
+          }
+        }
+      }
+    }
+    // (b) busy entries: lane = source, one entry at a time
+    uint32_t dense = __ballot_sync(kFull, !sparse && cnt > 0);
+    while (dense) {
+      const int32_t j = __ffs(dense) - 1;
+      dense &= dense - 1;
+      const int32_t uj = __shfl_sync(kFull, u, j);
+      const int32_t bj = __shfl_sync(kFull, b, j);
+      const int32_t eend = bj + __shfl_sync(kFull, cnt, j);
+      const uint32_t mj = __shfl_sync(kFull, m, j);
+      const bool act = (mj >> lane) & 1u;
+      const int32_t du = act ? __ldcg(S.dist + (int64_t)uj * kLanes + lane) : INT_MAX;
+      const bool live = act && du != INT_MAX;
+      for (int32_t k0 = bj; k0 < eend; k0 += 32) {
+        int32_t vv = 0, ww = 0;
+        if (k0 + lane < eend) {
+          vv = __ldg(S.dst + k0 + lane);
+          ww = __ldg(S.w + k0 + lane);
+        }
+        const int32_t cn = min(32, eend - k0);
+        for (int32_t j0 = 0; j0 < cn; j0 += kPrefetch) {
+          // Issue the distance-line loads of kPrefetch edges before using
+          // them.  A stale (larger) value only costs an extra atomicMin.
+          int32_t vs[kPrefetch], ws[kPrefetch], dvs[kPrefetch];
+#pragma unroll
+          for (int32_t t = 0; t < kPrefetch; ++t) {
+            vs[t] = __shfl_sync(kFull, vv, (j0 + t) & 31);
+            ws[t] = __shfl_sync(kFull, ww, (j0 + t) & 31);
+            dvs[t] = (live && j0 + t < cn) ? __ldcg(S.dist + (int64_t)vs[t] * kLanes + lane) : INT_MIN;
+          }
+#pragma unroll
+          for (int32_t t = 0; t < kPrefetch; ++t) {
+            if (j0 + t >= cn) break;  // warp-uniform
+            const int32_t v = vs[t];
+            bool near = false, farb = false;
+            if (live) {
+              const int32_t np = du + ws[t];
+              if (np < dvs[t] && atomicMin(S.dist + (int64_t)v * kLanes + lane, np) > np) {
+                near = np < cut;
+                farb = !near;
+              }
+            }
+            const uint32_t nb = __ballot_sync(kFull, near);
+            const uint32_t fb = __ballot_sync(kFull, farb);
+            if (lane == 0) {
+              if (nb) {
+                atomicOr(S.nacc + v, nb);
+                if (atomicMax(S.qstamp + v, it) < it) bs_enqueue(S, qo, qcnt_out, v);
+              }
+              if (fb && atomicOr(S.far + v, fb) == 0u) bs_far_push(S, p, v);
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
   __shared__ int32_t red[256 / 32][kLanes];
+  __shared__ int32_t s_cut[kLanes];
   const int32_t lane = threadIdx.x & 31;
   const int32_t wib = threadIdx.x >> 5;
   const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -62,6 +217,7 @@ __global__ void __launch_bounds__(256) k_bsssp(BsState S) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       S.cnt[(it + 1) % 3] = 0;
       S.cnt[5 + (it + 1) % 3] = 0;
+      S.wctr[(it + 1) % 3] = 0;
     }
     const int p = (int)(adv & 1);
     // ---- relax
@@ -69,96 +225,9 @@ __global__ void __launch_bounds__(256) k_bsssp(BsState S) {
       const int32_t curl = __ldcg(S.cur + p * kLanes + lane);
       const int64_t cl = (int64_t)curl + S.delta;
       const int32_t cut = cl > INT_MAX ? INT_MAX : (int32_t)cl;
-      const int64_t *qi = S.q[in];
-      int64_t *qo = S.q[in ^ 1];
-      for (int64_t e = gwarp; e < n; e += nwarps) {
-        const int64_t item = __ldcg(qi + e);
-        const int32_t u = (int32_t)(item >> 32);
-        const int32_t c = (int32_t)(item & 0xffffffff);
-        const uint32_t m = __ldcg(S.fr + u);
-        if (!m) continue;
-        const bool act = (m >> lane) & 1u;
-        const int32_t du = act ? __ldcg(S.dist + (int64_t)u * kLanes + lane) : INT_MAX;
-        const int32_t b = S.off[u] + c * S.chunk;
-        const int32_t eend = min(b + S.chunk, S.off[u + 1]);
-        if (__popc(m) <= S.ep_max) {
-          // Few active sources: lanes take edges, the warp loops over sources.
-          uint32_t mm = m;
-          while (mm) {
-            const int32_t s = __ffs(mm) - 1;
-            mm &= mm - 1;
-            const int32_t du_s = __shfl_sync(0xffffffffu, du, s);
-            const int32_t cut_s = __shfl_sync(0xffffffffu, cut, s);
-            if (du_s == INT_MAX) continue;
-            for (int32_t k = b + lane; k < eend; k += 32) {
-              const int32_t v = __ldg(S.dst + k);
-              const int32_t np = du_s + __ldg(S.w + k);
-              int32_t *pd = S.dist + (int64_t)v * kLanes + s;
-              if (np < __ldcg(pd) && atomicMin(pd, np) > np) {
-                if (np < cut_s) {
-                  atomicOr(S.nacc + v, 1u << s);
-                  if (atomicMax(S.qstamp + v, it) < it) bs_enqueue(S, qo, qcnt_out, v);
-                } else if (atomicOr(S.far + v, 1u << s) == 0u) {
-                  const int32_t pos = atomicAdd(S.cnt + 3 + p, 1);
-                  if (pos < S.V)
-                    S.fl[p][pos] = v;
-                  else
-                    atomicOr(S.err, DEV_ERR_OVERFLOW);
-                }
-              }
-            }
-          }
-          continue;
-        }
-        for (int32_t k0 = b; k0 < eend; k0 += 32) {
-          int32_t vv = 0, ww = 0;
-          if (k0 + lane < eend) {
-            vv = __ldg(S.dst + k0 + lane);
-            ww = __ldg(S.w + k0 + lane);
-          }
-          const int32_t cnt = min(32, eend - k0);
-          const bool live = act && du != INT_MAX;
-          for (int32_t j0 = 0; j0 < cnt; j0 += kPrefetch) {
-            // Issue the distance-line loads of kPrefetch edges before using
-            // them.  A stale (larger) value only costs an extra atomicMin.
-            int32_t vs[kPrefetch], ws[kPrefetch], dvs[kPrefetch];
-#pragma unroll
-            for (int32_t t = 0; t < kPrefetch; ++t) {
-              vs[t] = __shfl_sync(0xffffffffu, vv, (j0 + t) & 31);
-              ws[t] = __shfl_sync(0xffffffffu, ww, (j0 + t) & 31);
-              dvs[t] = (live && j0 + t < cnt) ? __ldcg(S.dist + (int64_t)vs[t] * kLanes + lane) : INT_MIN;
-            }
-#pragma unroll
-            for (int32_t t = 0; t < kPrefetch; ++t) {
-              if (j0 + t >= cnt) break;  // warp-uniform
-              const int32_t v = vs[t];
-              bool near = false, farb = false;
-              if (live) {
-                const int32_t np = du + ws[t];
-                if (np < dvs[t] && atomicMin(S.dist + (int64_t)v * kLanes + lane, np) > np) {
-                  near = np < cut;
-                  farb = !near;
-                }
-              }
-              const uint32_t nb = __ballot_sync(0xffffffffu, near);
-              const uint32_t fb = __ballot_sync(0xffffffffu, farb);
-              if (lane == 0) {
-                if (nb) {
-                  atomicOr(S.nacc + v, nb);
-                  if (atomicMax(S.qstamp + v, it) < it) bs_enqueue(S, qo, qcnt_out, v);
-                }
-                if (fb && atomicOr(S.far + v, fb) == 0u) {
-                  const int32_t pos = atomicAdd(S.cnt + 3 + p, 1);
-                  if (pos < S.V)
-                    S.fl[p][pos] = v;
-                  else
-                    atomicOr(S.err, DEV_ERR_OVERFLOW);
-                }
-              }
-            }
-          }
-        }
-      }
+      if (threadIdx.x < kLanes) s_cut[threadIdx.x] = cut;
+      __syncthreads();
+      bs_relax(S, n, S.q[in], S.q[in ^ 1], qcnt_out, cut, s_cut, p, it, S.wctr + it % 3, nwarps);
     }
     if (!grid_barrier(S.bar, gridDim.x, S.err, S.timeout_ns)) break;
     // ---- publish near masks of the queued vertices; OR them into the active set
@@ -179,7 +248,7 @@ __global__ void __launch_bounds__(256) k_bsssp(BsState S) {
         }
         act |= x;
       }
-      act = __reduce_or_sync(0xffffffffu, act);
+      act = __reduce_or_sync(kFull, act);
       if (lane == 0 && act) atomicOr(reinterpret_cast<uint32_t *>(S.cnt + 5 + it % 3), act);
     }
     clk.tick(S.stop);
@@ -188,12 +257,12 @@ __global__ void __launch_bounds__(256) k_bsssp(BsState S) {
     uint32_t unfinished = 0;
     {
       const int32_t cv = __ldcg(S.cur + p * kLanes + lane);
-      unfinished = __ballot_sync(0xffffffffu, cv != INT_MAX);
+      unfinished = __ballot_sync(kFull, cv != INT_MAX);
     }
     const uint32_t active = (uint32_t)*(volatile int32_t *)(S.cnt + 5 + it % 3);
     const uint32_t A = unfinished & ~active;
     if (A) {
-      const int32_t fcount = *(volatile int32_t *)(S.cnt + 3 + p);
+      const int32_t fcount = min(*(volatile int32_t *)(S.cnt + 3 + p), S.V);
       const int32_t *fla = S.fl[p];
       const int32_t curl = __ldcg(S.cur + p * kLanes + lane);
       const int64_t window = (int64_t)curl + S.delta;
@@ -202,65 +271,122 @@ __global__ void __launch_bounds__(256) k_bsssp(BsState S) {
         S.gmin[(p ^ 1) * kLanes + threadIdx.x] = INT_MAX;
         if (threadIdx.x == 0) S.cnt[3 + (p ^ 1)] = 0;
       }
-      // pass 1: per-source minimum far priority at or above the window
+      // pass 1: per-source minimum far priority at or above the window.
+      // Lane l loads far entry l of the warp's 32; the distance lines of the
+      // entries with advancing sources are then loaded 4 at a time.
       int32_t mn = INT_MAX;
-      for (int64_t e = gwarp; e < fcount; e += nwarps) {
-        const int32_t v = __ldcg(fla + e);
-        const uint32_t fm = __ldcg(S.far + v);
-        if (adv_l && ((fm >> lane) & 1u)) {
-          const int32_t d = __ldcg(S.dist + (int64_t)v * kLanes + lane);
-          if ((int64_t)d >= window && d < mn) mn = d;
+      const int32_t FB = bs_batch(fcount, nwarps);
+      for (int64_t e0 = gwarp * FB; e0 < fcount; e0 += nwarps * FB) {
+        const int64_t e = e0 + lane;
+        int32_t vl = 0;
+        uint32_t fml = 0;
+        if (lane < FB && e < fcount) {
+          vl = __ldcg(fla + e);
+          fml = __ldcg(S.far + vl) & A;
+        }
+        uint32_t want = __ballot_sync(kFull, fml != 0u);
+        while (want) {
+          int32_t vs[4];
+          bool hs[4];
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            int32_t j = 0;
+            if (want) {
+              j = __ffs(want) - 1;
+              want &= want - 1;
+              hs[t] = (__shfl_sync(kFull, fml, j) >> lane) & 1u;
+            } else {
+              __shfl_sync(kFull, fml, 0);
+              hs[t] = false;
+            }
+            vs[t] = __shfl_sync(kFull, vl, j);
+          }
+          int32_t ds[4];
+#pragma unroll
+          for (int t = 0; t < 4; ++t) ds[t] = hs[t] ? __ldcg(S.dist + (int64_t)vs[t] * kLanes + lane) : INT_MAX;
+#pragma unroll
+          for (int t = 0; t < 4; ++t)
+            if (hs[t] && (int64_t)ds[t] >= window && ds[t] < mn) mn = ds[t];
         }
       }
       red[wib][lane] = mn;
       __syncthreads();
       if (threadIdx.x < kLanes) {
-        int32_t m = INT_MAX;
-        for (int32_t k = 0; k < (int32_t)(blockDim.x >> 5); ++k) m = min(m, red[k][threadIdx.x]);
-        if (m != INT_MAX) atomicMin(S.gmin + p * kLanes + threadIdx.x, m);
+        int32_t mm = INT_MAX;
+        for (int32_t k = 0; k < (int32_t)(blockDim.x >> 5); ++k) mm = min(mm, red[k][threadIdx.x]);
+        if (mm != INT_MAX) atomicMin(S.gmin + p * kLanes + threadIdx.x, mm);
       }
       if (!grid_barrier(S.bar, gridDim.x, S.err, S.timeout_ns)) break;
       // pass 2: move [cur', cur'+delta) to the near frontier, keep the rest
-      const int32_t g = __ldcg(S.gmin + p * kLanes + lane);
-      const int32_t newcur = adv_l ? g : curl;
+      const int32_t gm = __ldcg(S.gmin + p * kLanes + lane);
+      const int32_t newcur = adv_l ? gm : curl;
       const int64_t hi = (int64_t)newcur + S.delta;
       int64_t *qo = S.q[in ^ 1];
-      for (int64_t e = gwarp; e < fcount; e += nwarps) {
-        const int32_t v = __ldcg(fla + e);
-        const uint32_t fm = __ldcg(S.far + v);
-        const bool f = (fm >> lane) & 1u;
-        bool keep = false, move = false;
-        if (f) {
-          if (!adv_l) {
-            keep = true;
-          } else if (newcur != INT_MAX) {
-            const int32_t d = __ldcg(S.dist + (int64_t)v * kLanes + lane);
-            if ((int64_t)d >= window) {
-              if ((int64_t)d < hi)
-                move = true;
-              else
-                keep = true;
+      for (int64_t e0 = gwarp * FB; e0 < fcount; e0 += nwarps * FB) {
+        const int64_t e = e0 + lane;
+        const bool mine = lane < FB && e < fcount;
+        int32_t vl = 0;
+        uint32_t fml = 0;
+        if (mine) {
+          vl = __ldcg(fla + e);
+          fml = __ldcg(S.far + vl);
+        }
+        uint32_t rem = fml & ~A;  // far bits of sources that do not advance stay
+        uint32_t mv = 0;
+        uint32_t todo = __ballot_sync(kFull, (fml & A) != 0u);
+        while (todo) {
+          int32_t js[4], vs[4];
+          bool hs[4];
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            js[t] = -1;
+            int32_t j = 0;
+            if (todo) {
+              j = __ffs(todo) - 1;
+              todo &= todo - 1;
+              js[t] = j;
+            }
+            const uint32_t fm = __shfl_sync(kFull, fml, j);
+            vs[t] = __shfl_sync(kFull, vl, j);
+            hs[t] = js[t] >= 0 && adv_l && ((fm >> lane) & 1u) && newcur != INT_MAX;
+          }
+          int32_t ds[4];
+#pragma unroll
+          for (int t = 0; t < 4; ++t) ds[t] = hs[t] ? __ldcg(S.dist + (int64_t)vs[t] * kLanes + lane) : 0;
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            const bool in_win = hs[t] && (int64_t)ds[t] >= window;
+            const bool keep = in_win && (int64_t)ds[t] >= hi;
+            const bool move = in_win && (int64_t)ds[t] < hi;
+            const uint32_t kb = __ballot_sync(kFull, keep);
+            const uint32_t mb = __ballot_sync(kFull, move);
+            if (lane == js[t]) {
+              rem |= kb;
+              mv = mb;
             }
           }
         }
-        const uint32_t rem = __ballot_sync(0xffffffffu, keep);
-        const uint32_t mv = __ballot_sync(0xffffffffu, move);
-        if (lane == 0) {
-          S.far[v] = rem;
-          if (rem) {
-            const int32_t pos = atomicAdd(S.cnt + 3 + (p ^ 1), 1);
+        if (mine) S.far[vl] = rem;
+        const bool app = mine && rem != 0u;
+        const uint32_t am = __ballot_sync(kFull, app);
+        if (am) {
+          int32_t base = 0;
+          if (lane == 0) base = atomicAdd(S.cnt + 3 + (p ^ 1), __popc(am));
+          base = __shfl_sync(kFull, base, 0);
+          if (app) {
+            const int32_t pos = base + __popc(am & ((1u << lane) - 1u));
             if (pos < S.V)
-              S.fl[p ^ 1][pos] = v;
+              S.fl[p ^ 1][pos] = vl;
             else
               atomicOr(S.err, DEV_ERR_OVERFLOW);
           }
-          if (mv) {
-            if (atomicMax(S.qstamp + v, it) < it) {
-              S.fr[v] = mv;
-              bs_enqueue(S, qo, qcnt_out, v);
-            } else {
-              atomicOr(S.fr + v, mv);
-            }
+        }
+        if (mine && mv) {
+          if (atomicMax(S.qstamp + vl, it) < it) {
+            S.fr[vl] = mv;
+            bs_enqueue(S, qo, qcnt_out, vl);
+          } else {
+            atomicOr(S.fr + vl, mv);
           }
         }
       }
@@ -294,6 +420,7 @@ __global__ void k_bsssp_init(BsState S, const int32_t *__restrict__ srcs, int32_
 __global__ void k_bsssp_seed(BsState S, const int32_t *__restrict__ srcs, int32_t nsrc) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   for (int32_t i = 0; i < 8; ++i) S.cnt[i] = 0;
+  for (int32_t i = 0; i < 3; ++i) S.wctr[i] = 0;
   *S.stop = 0;
   for (int32_t s = 0; s < kLanes; ++s) {
     S.cur[s] = s < nsrc ? 0 : INT_MAX;
@@ -362,6 +489,7 @@ BsState bsssp_state(gg_graph *g, const BsBuffers &b, int32_t delta) {
   S.gmin = hdr + 72;        // 64
   S.stats = hdr + 136;      // 2
   S.stop = hdr + 140;
+  S.wctr = hdr + 144;       // 3
   S.q[0] = b.queues;
   S.q[1] = b.queues + b.qcap;
   S.qcap = b.qcap;
