@@ -17,8 +17,16 @@
 // is at or above the window was last improved at or above a cutoff, so the far
 // list holds exactly the candidates the reference finds by scanning all V.
 //
+// A relaxation registers (near or far) when its value is below the distance
+// read before its atomicMin, which is issued without waiting for the old value:
+// a concurrent smaller write can only make the registration redundant, never
+// lose one.  The first thread to set a near bit of v in an iteration (its
+// atomicOr on the near mask returns 0) queues v.
+//
 // Iteration: relax | barrier | publish near masks, collect the active sources |
 // barrier | [advance pass 1 (minima) | barrier | pass 2 (move/keep) | barrier].
+#include <cooperative_groups/scan.h>
+
 #include <algorithm>
 
 #include "batch.h"
@@ -33,10 +41,17 @@ constexpr int32_t kPrefetch = 8;  // distance lines in flight per warp
 
 constexpr uint32_t kFull = 0xffffffffu;
 
+// Queues v as ceil(deg/chunk) entries.  The threads of a warp that enqueue
+// together reserve their entries with one atomic (coalesced-group scan).
 __device__ __forceinline__ void bs_enqueue(const BsState &S, int64_t *q, int32_t *qcnt, int32_t v) {
   const int32_t deg = S.off[v + 1] - S.off[v];
   const int32_t nch = max(1, ceil_div(deg, S.chunk));
-  const int32_t pos = atomicAdd(qcnt, nch);
+  cg::coalesced_group grp = cg::coalesced_threads();
+  const int32_t excl = cg::exclusive_scan(grp, nch);
+  const uint32_t last = grp.size() - 1;
+  int32_t base = 0;
+  if (grp.thread_rank() == last) base = atomicAdd(qcnt, excl + nch);
+  const int32_t pos = grp.shfl(base, last) + excl;
   if ((int64_t)pos + nch > S.qcap) {
     atomicOr(S.err, DEV_ERR_OVERFLOW);
     return;
@@ -51,7 +66,7 @@ __device__ __forceinline__ int32_t bs_batch(int64_t n, int64_t nwarps) {
 }
 
 __device__ __forceinline__ void bs_far_push(const BsState &S, int p, int32_t v) {
-  const int32_t pos = atomicAdd(S.cnt + 3 + p, 1);
+  const int32_t pos = agg_inc(S.cnt + 3 + p);
   if (pos < S.V)
     S.fl[p][pos] = v;
   else
@@ -127,10 +142,13 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n, const int6
             if (du == INT_MAX) continue;
             const int32_t np = du + w;
             int32_t *pd = S.dist + (int64_t)v * kLanes + s;
-            if (np < __ldcg(pd) && atomicMin(pd, np) > np) {
+            if (np < __ldcg(pd)) {
+              atomicMin(pd, np);
               if (np < s_cut[s]) {
-                atomicOr(S.nacc + v, 1u << s);
-                if (atomicMax(S.qstamp + v, it) < it) bs_enqueue(S, qo, qcnt_out, v);
+                if (atomicOr(S.nacc + v, 1u << s) == 0u) {
+                  S.qstamp[v] = it;
+                  bs_enqueue(S, qo, qcnt_out, v);
+                }
               } else if (atomicOr(S.far + v, 1u << s) == 0u) {
                 bs_far_push(S, p, v);
               }
@@ -168,28 +186,35 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n, const int6
             ws[t] = __shfl_sync(kFull, ww, (j0 + t) & 31);
             dvs[t] = (live && j0 + t < cn) ? __ldcg(S.dist + (int64_t)vs[t] * kLanes + lane) : INT_MIN;
           }
+          // lane t collects edge t's near / far source masks; the vertex
+          // updates of the kPrefetch edges then run on lanes 0..kPrefetch-1
+          int32_t my_v = 0;
+          uint32_t my_nb = 0, my_fb = 0;
 #pragma unroll
           for (int32_t t = 0; t < kPrefetch; ++t) {
             if (j0 + t >= cn) break;  // warp-uniform
-            const int32_t v = vs[t];
             bool near = false, farb = false;
             if (live) {
               const int32_t np = du + ws[t];
-              if (np < dvs[t] && atomicMin(S.dist + (int64_t)v * kLanes + lane, np) > np) {
+              if (np < dvs[t]) {
+                atomicMin(S.dist + (int64_t)vs[t] * kLanes + lane, np);
                 near = np < cut;
                 farb = !near;
               }
             }
             const uint32_t nb = __ballot_sync(kFull, near);
             const uint32_t fb = __ballot_sync(kFull, farb);
-            if (lane == 0) {
-              if (nb) {
-                atomicOr(S.nacc + v, nb);
-                if (atomicMax(S.qstamp + v, it) < it) bs_enqueue(S, qo, qcnt_out, v);
-              }
-              if (fb && atomicOr(S.far + v, fb) == 0u) bs_far_push(S, p, v);
+            if (lane == t) {
+              my_v = vs[t];
+              my_nb = nb;
+              my_fb = fb;
             }
           }
+          if (my_nb && atomicOr(S.nacc + my_v, my_nb) == 0u) {
+            S.qstamp[my_v] = it;
+            bs_enqueue(S, qo, qcnt_out, my_v);
+          }
+          if (my_fb && atomicOr(S.far + my_v, my_fb) == 0u) bs_far_push(S, p, my_v);
         }
       }
     }
@@ -366,7 +391,7 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
             }
           }
         }
-        if (mine) S.far[vl] = rem;
+        if (mine && rem != fml) S.far[vl] = rem;
         const bool app = mine && rem != 0u;
         const uint32_t am = __ballot_sync(kFull, app);
         if (am) {
