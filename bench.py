@@ -44,7 +44,7 @@ METRIC = "GTEPS per app at 1 GB300: learned+batched vs plain schedule, exact res
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=40)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     p.add_argument("--scale", type=int, default=SCALE)

@@ -77,6 +77,7 @@ SIGNATURES: dict[str, tuple] = {
     "gg_set_default_launch": (None, [i32, i32]),
     "gg_host_graph_rmat": (i32, [i32, i32, f32, f32, f32, i64, i32, i32, i32, C.POINTER(P)]),
     "gg_host_graph_grid": (i32, [i32, i32, i64, i32, i32, C.POINTER(P)]),
+    "gg_host_graph_mix_spec": (i32, [i64, i32, P]),
     "gg_host_graph_from_edges": (i32, [i32, i64, P, P, P, i32, C.POINTER(P)]),
     "gg_host_graph_from_csr": (i32, [i32, i64, P, P, P, C.POINTER(P)]),
     "gg_host_graph_load": (i32, [C.c_char_p, i32, C.POINTER(P)]),

@@ -83,6 +83,16 @@ def build_lib(verbose: bool = False, jobs: int | None = None) -> Path:
     return LIB
 
 
+def build_cli() -> Path:
+    """Builds easy_graphit_gb300/gg_app, the apps' trial-loop driver (links libgg.so)."""
+    src = PKG / "cli" / "gg_app.cpp"
+    exe = PKG / "gg_app"
+    if not exe.exists() or any(p.stat().st_mtime > exe.stat().st_mtime for p in [src, LIB, *INCLUDE.glob("*.h")]):
+        _run(["g++", "-std=c++17", "-O2", "-Wall", f"-I{INCLUDE}", str(src), "-o", str(exe),
+              f"-L{PKG}", "-lgg", "-Wl,-rpath,$ORIGIN"])
+    return exe
+
+
 def build_oracle() -> Path:
     """Compiles the oracle's CPU restatement (test infrastructure)."""
     _run(["make", "-s", "-C", str(ORACLE), "all"])
@@ -101,5 +111,6 @@ def build_ref_oracle() -> Path | None:
 
 if __name__ == "__main__":
     print(build_lib(verbose=True))
+    print(build_cli())
     print(build_oracle())
     print(build_ref_oracle())

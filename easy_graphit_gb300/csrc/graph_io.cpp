@@ -499,6 +499,28 @@ gg_status gg_host_graph_pick_sources(const gg_host_graph *g, int32_t n, int64_t 
   return GG_OK;
 }
 
+gg_status gg_host_graph_mix_spec(int64_t seed, int32_t count, int32_t *spec) {
+  GG_CHECK_ARG(spec && count >= 0, "bad arguments");
+  // One std::mt19937(seed) draws, per graph, a kind (grid with probability
+  // 1/4), then a grid side 2^[8,11] or an R-MAT scale [12,20] and edge factor
+  // [4,32]; each graph's own generator seed is seed + 1 + its index.
+  std::mt19937 rng((std::mt19937::result_type)seed);
+  std::uniform_int_distribution<int32_t> kind(0, 3), side(8, 11), scale(12, 20), ef(4, 32);
+  for (int32_t i = 0; i < count; ++i) {
+    int32_t *r = spec + 3 * (size_t)i;
+    if (kind(rng) == 0) {
+      r[0] = 1;
+      r[1] = 1 << side(rng);
+      r[2] = 0;
+    } else {
+      r[0] = 0;
+      r[1] = scale(rng);
+      r[2] = ef(rng);
+    }
+  }
+  return GG_OK;
+}
+
 gg_status gg_host_graph_info(const gg_host_graph *g, int32_t *num_vertices, int64_t *num_edges) {
   GG_CHECK_ARG(g, "graph is NULL");
   if (num_vertices) *num_vertices = g->V;

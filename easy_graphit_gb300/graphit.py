@@ -304,6 +304,26 @@ class HostGraph:
         call("gg_host_graph_union", arr, len(parts), _np_ptr(offs), C.byref(h))
         return cls(h), offs
 
+    @staticmethod
+    def mix_spec(count: int = 64, seed: int = K_RAND_SEED) -> np.ndarray:
+        """[count, 3] rows (0 R-MAT | 1 grid, scale | side, edge factor | 0) of the
+        batched mode's mix of uneven graphs, drawn from std::mt19937(seed)."""
+        spec = np.empty((count, 3), dtype=np.int32)
+        call("gg_host_graph_mix_spec", seed, count, _np_ptr(spec))
+        return spec
+
+    @classmethod
+    def mix(cls, count: int = 64, seed: int = K_RAND_SEED, symmetrize: bool = False) -> list["HostGraph"]:
+        """The graphs of mix_spec(count, seed); graph i uses generator seed
+        seed + 1 + i (grids are symmetric by construction)."""
+        out = []
+        for i, (kind, size, ef) in enumerate(cls.mix_spec(count, seed)):
+            if kind == 1:
+                out.append(cls.grid(int(size), int(size), seed=seed + 1 + i))
+            else:
+                out.append(cls.rmat(int(size), int(ef), seed=seed + 1 + i, symmetrize=symmetrize))
+        return out
+
     def pick_sources(self, n: int, seed: int = K_RAND_SEED) -> np.ndarray:
         """GAPBS SourcePicker (benchmark.h:50-71): n non-zero-degree vertices."""
         out = np.empty(n, dtype=np.int32)

@@ -147,6 +147,12 @@ gg_status gg_host_graph_union(const gg_host_graph *const *parts, int32_t n,
  * uniform ids from std::mt19937(seed), skipping vertices with no out-edges. */
 gg_status gg_host_graph_pick_sources(const gg_host_graph *g, int32_t n,
                                      int64_t seed, int32_t *out);
+/* The batched mode's mix of uneven graphs (no reference counterpart): count
+ * graphs drawn from std::mt19937(seed), each a 2-D grid with probability 1/4
+ * (side 256, 512, 1024 or 2048) or else an R-MAT graph with scale in [12, 20]
+ * and edge factor in [4, 32].  spec[i] = {0 R-MAT | 1 grid, scale | side,
+ * edge factor | 0}; graph i is generated with seed + 1 + i. */
+gg_status gg_host_graph_mix_spec(int64_t seed, int32_t count, int32_t *spec);
 const int32_t *gg_host_graph_offsets(const gg_host_graph *g);
 const int32_t *gg_host_graph_dst(const gg_host_graph *g);
 const int32_t *gg_host_graph_weights(const gg_host_graph *g);

@@ -40,3 +40,22 @@ def rel_l1(x, ref):
     x = np.asarray(x, dtype=np.float64)
     ref = np.asarray(ref, dtype=np.float64)
     return float(np.abs(x - ref).sum() / max(np.abs(ref).sum(), 1e-300))
+
+
+def shortest_paths_certified(off, dst, w, dist, src) -> bool:
+    """dist is the exact shortest-path distance array from src iff dist[src] = 0,
+    no edge can improve it (dist[v] <= dist[u] + w), and every other reached
+    vertex has a tight in-edge (dist[v] = dist[u] + w): with positive weights the
+    tight edges then lead back to src."""
+    V = len(off) - 1
+    u = np.repeat(np.arange(V, dtype=np.int64), np.diff(off))
+    du = dist[u].astype(np.int64)
+    dv = dist[dst].astype(np.int64)
+    reached_u = du != INT_MAX
+    if not np.all(~reached_u | (dv <= du + w)):
+        return False
+    tight = reached_u & (dv == du + w)
+    has_tight = np.bincount(dst[tight], minlength=V) > 0
+    reached = dist != INT_MAX
+    reached[src] = False
+    return bool(dist[src] == 0 and np.all(has_tight[reached]))

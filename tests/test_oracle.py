@@ -130,3 +130,21 @@ def test_sssp_matches_scipy(golden):
     d = csg.dijkstra(A, indices=s)
     ref = np.where(np.isinf(d), INT_MAX, d).astype(np.int64)
     np.testing.assert_array_equal(oracle.sssp_dijkstra(off, dst, w, s), ref)
+
+
+def test_shortest_path_certificate_accepts_exact_and_rejects_wrong_distances():
+    from easy_graphit_gb300 import HostGraph
+    from tests.conftest import shortest_paths_certified
+    hg = HostGraph.rmat(10, 8)
+    off, dst, w = np.array(hg.offsets), np.array(hg.dst), np.array(hg.weights)
+    s = int(hg.pick_sources(1)[0])
+    d = oracle.sssp_dijkstra(off, dst, w, s)
+    assert shortest_paths_certified(off, dst, w, d, s)
+    reached = np.flatnonzero((d != 2**31 - 1) & (np.arange(len(d)) != s))
+    bad = d.copy()
+    bad[reached[0]] -= 1                      # too small: no tight in-edge
+    assert not shortest_paths_certified(off, dst, w, bad, s)
+    bad = d.copy()
+    bad[reached[-1]] += 1                     # too large: an edge improves it
+    assert not shortest_paths_certified(off, dst, w, bad, s)
+    assert not shortest_paths_certified(off, dst, w, np.zeros_like(d), s)
