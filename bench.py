@@ -51,8 +51,9 @@ def parse():
     p.add_argument("--delta", type=int, default=32,
                    help="delta-stepping bucket width (both arms); 0 = autotune over {1,8,32,128}")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--tuning", choices=["auto", "default"], default="auto",
-                   help="launch shape of the batched kernels: autotuned on the graph, or the built-in one")
+    p.add_argument("--tuning", default="auto",
+                   help="launch shape of the batched kernel: 'auto' (autotuned on the graph), 'default' "
+                        "(built-in) or 'B,C,E' (CTAs per SM, chunk, edge-parallel threshold)")
     p.add_argument("--no-apps", action="store_true",
                    help="omit the per-app comparison lines (BFS, BC, PageRank)")
     return p.parse_args()
@@ -211,7 +212,7 @@ def run_gb300(args):
     import torch.distributed as dist
 
     from easy_graphit_gb300 import (GraphT, LearnedGPUSchedule, Selector, _lib as L, app_schedule,
-                                    autotune_batch, default_schedule)
+                                    autotune_batch, default_schedule, set_batch_tuning)
     from easy_graphit_gb300 import SimpleGPUSchedule as T
     from easy_graphit_gb300.replicas import aggregate_teps, rank_sources
 
@@ -257,6 +258,10 @@ def run_gb300(args):
     tuned, tune_rows = None, []
     if args.tuning == "auto":
         tuned, tune_rows = autotune_batch(g, "sssp", h_src, delta)
+    elif args.tuning != "default":
+        b_, c_, e_ = (int(x) for x in args.tuning.split(","))
+        set_batch_tuning(g, "sssp", b_, c_, e_)
+        tuned = {"blocks_per_sm": b_, "chunk": c_, "edge_parallel_max": e_}
 
     # Algorithmic work per source (untimed): E_r, V_r from the distances.
     batched(delta, base)
