@@ -134,23 +134,36 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n, const int6
         if (idx < total) {
           const int32_t k = bj + (idx - exj);
           const int32_t v = __ldg(S.dst + k), w = __ldg(S.w + k);
+          // the entry's sources four at a time: their u and v distance loads
+          // are issued together
           uint32_t mm = mj;
           while (mm) {
-            const int32_t s = __ffs(mm) - 1;
-            mm &= mm - 1;
-            const int32_t du = __ldcg(S.dist + (int64_t)uj * kLanes + s);
-            if (du == INT_MAX) continue;
-            const int32_t np = du + w;
-            int32_t *pd = S.dist + (int64_t)v * kLanes + s;
-            if (np < __ldcg(pd)) {
-              atomicMin(pd, np);
-              if (np < s_cut[s]) {
-                if (atomicOr(S.nacc + v, 1u << s) == 0u) {
-                  S.qstamp[v] = it;
-                  bs_enqueue(S, qo, qcnt_out, v);
+            int32_t ss[4], du[4], dv[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+              ss[t] = mm ? __ffs(mm) - 1 : -1;
+              mm &= mm - 1;
+            }
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+              du[t] = ss[t] >= 0 ? __ldcg(S.dist + (int64_t)uj * kLanes + ss[t]) : INT_MAX;
+              dv[t] = ss[t] >= 0 ? __ldcg(S.dist + (int64_t)v * kLanes + ss[t]) : INT_MIN;
+            }
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+              if (du[t] == INT_MAX) continue;
+              const int32_t s = ss[t];
+              const int32_t np = du[t] + w;
+              if (np < dv[t]) {
+                atomicMin(S.dist + (int64_t)v * kLanes + s, np);
+                if (np < s_cut[s]) {
+                  if (atomicOr(S.nacc + v, 1u << s) == 0u) {
+                    S.qstamp[v] = it;
+                    bs_enqueue(S, qo, qcnt_out, v);
+                  }
+                } else if (atomicOr(S.far + v, 1u << s) == 0u) {
+                  bs_far_push(S, p, v);
                 }
-              } else if (atomicOr(S.far + v, 1u << s) == 0u) {
-                bs_far_push(S, p, v);
               }
             }
           }
@@ -461,13 +474,22 @@ __global__ void k_bsssp_seed(BsState S, const int32_t *__restrict__ srcs, int32_
   }
 }
 
-__global__ void k_bsssp_out(const int32_t *__restrict__ dist, int32_t V, int32_t nsrc,
-                            int32_t *__restrict__ out) {
-  const int64_t total = (int64_t)nsrc * V;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t s = (int32_t)(i / V), v = (int32_t)(i % V);
-    out[i] = dist[(int64_t)v * kLanes + s];
+// Rows out[s][v] = dist[v][s] for s < nsrc, through 32 x 32 shared-memory
+// tiles so both the vertex-major reads and the row writes are coalesced.
+__global__ void __launch_bounds__(256) k_bsssp_out(const int32_t *__restrict__ dist, int32_t V, int32_t nsrc,
+                                                   int32_t *__restrict__ out) {
+  __shared__ int32_t tile[kLanes][33];
+  for (int64_t v0 = (int64_t)blockIdx.x * 32; v0 < V; v0 += (int64_t)gridDim.x * 32) {
+    for (int32_t i = threadIdx.x; i < 32 * kLanes; i += blockDim.x) {
+      const int32_t vv = i / kLanes, s = i % kLanes;
+      tile[s][vv] = v0 + vv < V ? dist[(v0 + vv) * kLanes + s] : 0;
+    }
+    __syncthreads();
+    for (int32_t i = threadIdx.x; i < 32 * nsrc; i += blockDim.x) {
+      const int32_t s = i / 32, vv = i % 32;
+      if (v0 + vv < V) out[(int64_t)s * V + v0 + vv] = tile[s][vv];
+    }
+    __syncthreads();
   }
 }
 
