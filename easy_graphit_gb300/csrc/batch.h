@@ -65,6 +65,7 @@ struct BsState {
   int32_t *stop;              // raised by block 0 when the loop's time limit passes
   uint64_t loop_limit_ns;
   int32_t *wctr;              // [3] relax work counters (rotating)
+  const int32_t *perm;        // original id -> id in the degree-ordered graph the kernel walks
 };
 
 // Device buffers of one batched-SSSP pass; `owned` buffers are freed with it,

@@ -467,22 +467,23 @@ __global__ void k_bsssp_seed(BsState S, const int32_t *__restrict__ srcs, int32_
     S.gmin[kLanes + s] = INT_MAX;
   }
   for (int32_t s = 0; s < nsrc; ++s) {
-    const int32_t v = srcs[s];
+    const int32_t v = S.perm[srcs[s]];
     S.dist[(int64_t)v * kLanes + s] = 0;
     if (!S.fr[v]) bs_enqueue(S, S.q[0], S.cnt + 0, v);
     S.fr[v] |= 1u << s;
   }
 }
 
-// Rows out[s][v] = dist[v][s] for s < nsrc, through 32 x 32 shared-memory
-// tiles so both the vertex-major reads and the row writes are coalesced.
-__global__ void __launch_bounds__(256) k_bsssp_out(const int32_t *__restrict__ dist, int32_t V, int32_t nsrc,
-                                                   int32_t *__restrict__ out) {
+// Rows out[s][v] = dist[perm[v]][s] for s < nsrc (v an original id), through
+// 32 x 32 shared-memory tiles so the distance-line reads and the row writes are
+// both coalesced.
+__global__ void __launch_bounds__(256) k_bsssp_out(const int32_t *__restrict__ dist, const int32_t *__restrict__ perm,
+                                                   int32_t V, int32_t nsrc, int32_t *__restrict__ out) {
   __shared__ int32_t tile[kLanes][33];
   for (int64_t v0 = (int64_t)blockIdx.x * 32; v0 < V; v0 += (int64_t)gridDim.x * 32) {
     for (int32_t i = threadIdx.x; i < 32 * kLanes; i += blockDim.x) {
       const int32_t vv = i / kLanes, s = i % kLanes;
-      tile[s][vv] = v0 + vv < V ? dist[(v0 + vv) * kLanes + s] : 0;
+      tile[s][vv] = v0 + vv < V ? dist[(int64_t)perm[v0 + vv] * kLanes + s] : 0;
     }
     __syncthreads();
     for (int32_t i = threadIdx.x; i < 32 * nsrc; i += blockDim.x) {
@@ -501,6 +502,7 @@ BsBuffers::~BsBuffers() {
 }
 
 gg_status bsssp_buffers(gg_graph *g, int32_t nsrc, bool owned, BsBuffers *b) {
+  GG_TRY(ensure_relabel(g));
   const int32_t V = g->csr.V;
   const int64_t E = g->csr.E;
   b->qcap = (int64_t)V + E / kMinChunk + 64;  // any tuning's chunk fits
@@ -540,9 +542,10 @@ BsState bsssp_state(gg_graph *g, const BsBuffers &b, int32_t delta) {
   S.q[0] = b.queues;
   S.q[1] = b.queues + b.qcap;
   S.qcap = b.qcap;
-  S.off = g->csr.off;
-  S.dst = g->csr.dst;
-  S.w = g->csr.w;
+  S.off = g->rel->g.off;  // the degree-ordered copy (bsssp_buffers built it)
+  S.dst = g->rel->g.dst;
+  S.w = g->rel->g.w;
+  S.perm = g->rel->perm;
   S.V = V;
   S.delta = delta;
   const gg_batch_tuning t = effective_tuning(g, GG_BATCH_SSSP, 1);
@@ -578,7 +581,7 @@ gg_status bsssp_enqueue(gg_graph *g, cudaStream_t st, const BsState &S, const in
   GG_CUDA(cudaLaunchCooperativeKernel((const void *)k_bsssp, bps * g->sm_count, 256, args, 0, st));
   if (timed) GG_CUDA(cudaEventRecord(g->ev3, st));
   note_launch();
-  k_bsssp_out<<<g->sm_count * 8, 256, 0, st>>>(S.dist, S.V, k, out_rows);
+  k_bsssp_out<<<g->sm_count * 8, 256, 0, st>>>(S.dist, S.perm, S.V, k, out_rows);
   GG_CUDA(cudaGetLastError());
   return GG_OK;
 }

@@ -22,6 +22,13 @@ struct GraphStore {
   DGraph view() const { return DGraph{V, E, off, dst, w, src, bucket, nbuckets}; }
 };
 
+// The graph renumbered by descending in-degree class (relabel.cu), with the
+// maps old -> new (perm) and new -> old (inv).
+struct Relabeled {
+  GraphStore g;
+  int32_t *perm = nullptr, *inv = nullptr;
+};
+
 // Scratch arena: grows on demand, reused across calls on the same graph.
 struct Scratch {
   void *p = nullptr;
@@ -34,6 +41,7 @@ struct gg_graph {
   gg::GraphStore csr;                        // forward CSR (+ COO src)
   std::unique_ptr<gg::GraphStore> csc;       // get_transposed_graph()
   std::map<int32_t, gg::GraphStore> blocked_fwd, blocked_rev;  // get_blocked_graph()
+  std::unique_ptr<gg::Relabeled> rel;        // degree-ordered copy for the batched kernels
   bool symmetric = false;
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
@@ -112,6 +120,10 @@ gg_status check_device_error(gg_graph *g, const char *what);
 gg_status scratch_get(gg_graph *g, int slot, size_t bytes, void **p);
 gg_status scratch_get_app(gg_graph *g, int slot, size_t bytes, void **p);
 int resident_grid(const void *kernel, int cta, size_t smem, int sm_count);
+
+// ---- relabel.cu
+gg_status ensure_relabel(gg_graph *g);
+void free_relabel(gg_graph *g);
 
 // ---- pagerank.cu
 gg_status pagerank_pull_twc(gg_graph *g, int32_t iters, float damping, float *rank, float *contrib2);

@@ -417,6 +417,7 @@ gg_status gg_graph_destroy(gg_graph *g) {
   if (g->csc) free_store(*g->csc, st);
   for (auto &kv : g->blocked_fwd) free_store(kv.second, st);
   for (auto &kv : g->blocked_rev) free_store(kv.second, st);
+  free_relabel(g);
   for (auto &s : g->scratch)
     if (s.p) cudaFreeAsync(s.p, st);
   for (void *p : {(void *)g->d_err, (void *)g->d_bar, (void *)g->d_misc})
