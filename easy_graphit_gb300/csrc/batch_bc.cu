@@ -48,6 +48,7 @@ struct BcState {
   uint16_t *depth;               // [V][64]
   double *sigma, *dep;           // [V][64]
   const int32_t *toff, *tsrc;    // in-neighbours (the CSR itself for a symmetric graph)
+  const int32_t *perm;           // original id -> walked id (degree-ordered copy), or null
   int32_t V, nsrc;
   uint32_t *bar;
   int32_t *err;
@@ -318,7 +319,7 @@ __global__ void k_bcb_seed(BcState st, const int32_t *__restrict__ srcs) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   int32_t n = 0;
   for (int32_t s = 0; s < st.nsrc; ++s) {
-    const int32_t v = srcs[s];
+    const int32_t v = st.perm ? st.perm[srcs[s]] : srcs[s];
     if (!st.seen[v]) st.lev[n++] = v;
     st.seen[v] |= 1ull << s;
     st.fr[0][v] |= 1ull << s;
@@ -329,9 +330,10 @@ __global__ void k_bcb_seed(BcState st, const int32_t *__restrict__ srcs) {
   *st.stop = 0;
 }
 
-// delta[s][v] = (dep'[v][s] - 1/sigma[v][s]) * sigma[v][s] as fp32 rows, via a
-// shared-memory transpose of 32-vertex tiles; also sums E_r over the sources
-// (out-degree times the number of sources that reached v).
+// delta[s][v] = (dep'[p][s] - 1/sigma[p][s]) * sigma[p][s] as fp32 rows (v an
+// original id, p its walked id), via a shared-memory transpose of 32-vertex
+// tiles; also sums E_r over the sources (out-degree times the number of sources
+// that reached v).
 __global__ void __launch_bounds__(256) k_bcb_out(BcState st, const int32_t *__restrict__ off, float *out,
                                                  int64_t out_stride, unsigned long long *reached) {
   __shared__ float tile[kBcWidth][33];
@@ -343,14 +345,16 @@ __global__ void __launch_bounds__(256) k_bcb_out(BcState st, const int32_t *__re
       const int32_t v = v0 + j;
       float r = 0.f;
       if (v < V) {
-        const double sg = st.sigma[(int64_t)v * kBcWidth + s];
-        if (sg != 0.0) r = (float)((st.dep[(int64_t)v * kBcWidth + s] - 1.0 / sg) * sg);
+        const int64_t pv = st.perm ? st.perm[v] : v;
+        const double sg = st.sigma[pv * kBcWidth + s];
+        if (sg != 0.0) r = (float)((st.dep[pv * kBcWidth + s] - 1.0 / sg) * sg);
       }
       tile[s][j] = r;
     }
     if (threadIdx.x < 32 && v0 + (int32_t)threadIdx.x < V) {
       const int32_t v = v0 + threadIdx.x;
-      er += (unsigned long long)__popcll(st.seen[v]) * (unsigned long long)(off[v + 1] - off[v]);
+      const int32_t pv = st.perm ? st.perm[v] : v;
+      er += (unsigned long long)__popcll(st.seen[pv]) * (unsigned long long)(off[v + 1] - off[v]);
     }
     __syncthreads();
     for (int32_t i = threadIdx.x; i < 32 * st.nsrc; i += blockDim.x) {
@@ -385,6 +389,7 @@ gg_status bcb_buffers(gg_graph *g, bool owned, BcBuffers *b) {
     return set_error(GG_ERR_UNSUPPORTED, "batched BC holds 64 level-list entries per vertex in int32: "
                                          "V = %d is too large (use gg_bc)", V);
   GG_TRY(ensure_transpose(g));
+  if (g->symmetric) GG_TRY(ensure_relabel(g));  // one degree-ordered copy serves both directions
   b->owned = owned;
   const size_t sz[6] = {sizeof(uint64_t) * 8 * (size_t)V, sizeof(int32_t) * bc_int_words(V),
                         sizeof(int64_t) * (size_t)bc_wcap(g), sizeof(uint16_t) * kBcWidth * (size_t)V,
@@ -406,8 +411,10 @@ gg_status bcb_buffers(gg_graph *g, bool owned, BcBuffers *b) {
 
 static BcState bcb_state(gg_graph *g, const BcBuffers &b, int32_t k) {
   const int32_t V = g->csr.V;
-  const GraphStore &t = g->csc ? *g->csc : g->csr;
+  const bool rel = g->symmetric && g->rel;
+  const GraphStore &t = rel ? g->rel->g : (g->csc ? *g->csc : g->csr);
   BcState S{};
+  S.perm = rel ? g->rel->perm : nullptr;
   S.seen = b.masks;
   S.acc = b.masks + V;
   S.rmask = b.masks + 2 * (size_t)V;
@@ -461,7 +468,7 @@ gg_status bcb_enqueue(gg_graph *g, cudaStream_t st, const BcBuffers &b, int32_t 
   note_launch();
   k_bcb_seed<<<1, 32, 0, st>>>(S, dsrc);
   GG_CUDA(cudaMemsetAsync(S.bar, 0, sizeof(uint32_t) * 2, st));
-  DGraph dg = g->csr.view();
+  DGraph dg = (g->symmetric && g->rel) ? g->rel->g.view() : g->csr.view();
   dg.nbuckets = 0;
   void *args[] = {&dg, &S};
   if (timed) GG_CUDA(cudaEventRecord(g->ev2, st));
