@@ -17,6 +17,7 @@ struct gg_batch_plan {
   gg::BsBuffers bs;
   gg::MsBfsBuffers ms;
   gg::BcBuffers bc;
+  int32_t *parent = nullptr;              // BFS multi-source: parent scratch
   unsigned long long *reached = nullptr;  // BC: reached out-edges summed over sources
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -27,6 +28,7 @@ struct gg_batch_plan {
     if (dsrc) cudaFree(dsrc);
     if (dstats) cudaFree(dstats);
     if (reached) cudaFree(reached);
+    if (parent) cudaFree(parent);
   }
 };
 
@@ -37,8 +39,9 @@ extern "C" {
 gg_status gg_batch_plan_create(gg_graph *g, int32_t app, const int32_t *sources, int32_t nsrc,
                                int32_t delta, void *out, gg_batch_plan **plan) {
   GG_CHECK_ARG(g && sources && nsrc > 0 && out && plan, "bad arguments");
-  GG_CHECK_ARG(app == GG_BATCH_BFS || app == GG_BATCH_SSSP || app == GG_BATCH_BC, "unknown batched app");
-  GG_CHECK_ARG(app != GG_BATCH_SSSP || delta >= 1, "delta must be >= 1");
+  GG_CHECK_ARG(app >= GG_BATCH_BFS && app <= GG_BATCH_SSSP_MULTI, "unknown batched app");
+  GG_CHECK_ARG((app != GG_BATCH_SSSP && app != GG_BATCH_SSSP_MULTI) || delta >= 1, "delta must be >= 1");
+  const bool multi = app == GG_BATCH_BFS_MULTI || app == GG_BATCH_SSSP_MULTI;
   cudaPointerAttributes pa{};
   if (cudaPointerGetAttributes(&pa, out) != cudaSuccess || pa.type != cudaMemoryTypeDevice)
     return set_error(GG_ERR_INVALID, "a batch plan writes into device memory; out is not device memory");
@@ -49,12 +52,15 @@ gg_status gg_batch_plan_create(gg_graph *g, int32_t app, const int32_t *sources,
   p->g = g;
   p->app = app;
   p->nsrc = nsrc;
-  const int32_t width = app == GG_BATCH_SSSP ? kBsLanes : kMsBfsWidth;
+  const int32_t width = multi ? nsrc : (app == GG_BATCH_SSSP ? kBsLanes : kMsBfsWidth);
   p->ngroups = ceil_div(nsrc, width);
   GG_CUDA(cudaMalloc(&p->dsrc, sizeof(int32_t) * nsrc));
   GG_CUDA(cudaMemcpy(p->dsrc, sources, sizeof(int32_t) * nsrc, cudaMemcpyDefault));
   GG_CUDA(cudaMalloc(&p->dstats, sizeof(int32_t) * 2 * p->ngroups));
-  if (app == GG_BATCH_BFS) {
+  if (multi) {
+    if (!g->app_frontier) GG_TRY(gg_frontier_create(g, 0, &g->app_frontier));
+    if (app == GG_BATCH_BFS_MULTI) GG_CUDA(cudaMalloc(&p->parent, sizeof(int32_t) * std::max(V, 1)));
+  } else if (app == GG_BATCH_BFS) {
     GG_TRY(msbfs_buffers(g, nsrc, true, &p->ms));
   } else if (app == GG_BATCH_SSSP) {
     GG_TRY(bsssp_buffers(g, nsrc, true, &p->bs));
@@ -73,7 +79,15 @@ gg_status gg_batch_plan_create(gg_graph *g, int32_t app, const int32_t *sources,
     const cudaError_t me = cudaMemsetAsync(p->reached, 0, sizeof(unsigned long long), cs);
     if (me != cudaSuccess) st = set_error(GG_ERR_CUDA, "memset in capture: %s", cudaGetErrorString(me));
   }
-  for (int32_t gi = 0; gi < p->ngroups && st == GG_OK; ++gi) {
+  if (multi) {
+    st = fused_multi_enqueue(g, cs, app == GG_BATCH_SSSP_MULTI, p->dsrc, nsrc, delta, p->parent, (int32_t *)out);
+    if (st == GG_OK) {
+      const cudaError_t ce2 = cudaMemcpyAsync(p->dstats, g->d_misc + 44, sizeof(int32_t) * 2,
+                                              cudaMemcpyDeviceToDevice, cs);
+      if (ce2 != cudaSuccess) st = set_error(GG_ERR_CUDA, "stats copy in capture: %s", cudaGetErrorString(ce2));
+    }
+  }
+  for (int32_t gi = 0; gi < p->ngroups && st == GG_OK && !multi; ++gi) {
     const int32_t base = gi * width;
     const int32_t k = std::min(width, nsrc - base);
     if (app == GG_BATCH_BFS) {
@@ -120,7 +134,7 @@ gg_status gg_batch_plan_run(gg_batch_plan *p, gg_stats *stats) {
     GG_CUDA(cudaMemcpy(h.data(), p->dstats, sizeof(int32_t) * h.size(), cudaMemcpyDeviceToHost));
     for (int32_t gi = 0; gi < p->ngroups; ++gi) {
       stats->iterations = std::max(stats->iterations, h[2 * gi]);
-      if (p->app == GG_BATCH_SSSP) stats->bucket_advances += h[2 * gi + 1];
+      if (p->app == GG_BATCH_SSSP || p->app == GG_BATCH_SSSP_MULTI) stats->bucket_advances += h[2 * gi + 1];
     }
     if (p->app == GG_BATCH_BC) {
       unsigned long long er = 0;

@@ -180,6 +180,10 @@ int32_t pq_cutoff(const gg_pq *pq);
 // *ran is false when the schedule has no device-side form (the caller then
 // runs the loop unfused).
 bool fused_supported(const gg_schedule *s);
+// Multi-source BFS (depth, parent scratch) or SSSP (dist) with the TWCE fused
+// loop, every step on the device (capturable); sources in device memory.
+gg_status fused_multi_enqueue(gg_graph *g, cudaStream_t st, bool sssp, const int32_t *dsrc, int32_t n,
+                              int32_t delta, int32_t *parent, int32_t *out);
 gg_status fused_bfs(gg_graph *g, const gg_schedule *s, int32_t n0, const VData &vd,
                     gg_frontier *f, int32_t *iters, bool *ran);
 gg_status fused_sssp(gg_graph *g, const gg_schedule *s, int32_t n0, int32_t delta, const VData &vd,

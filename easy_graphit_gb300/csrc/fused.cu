@@ -301,6 +301,77 @@ gg_status fused_sssp(gg_graph *g, const gg_schedule *s, int32_t n0, int32_t delt
   return GG_OK;
 }
 
+// ------------------------------------------------- capturable multi-source run
+// Reset of the vertex data, then the sources (device array) seeded into the
+// frontier queue and the loop's counters set, all on the device, so the whole
+// run is stream-ordered and can be captured into a CUDA graph.
+__global__ void k_multi_reset(VData vd, int32_t sssp, int32_t V) {
+  for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    if (sssp) {
+      vd.dist[v] = INT_MAX;
+    } else {
+      vd.parent[v] = -1;
+      vd.depth[v] = -1;
+    }
+  }
+}
+
+__global__ void k_multi_seed(VData vd, int32_t sssp, const int32_t *__restrict__ srcs, int32_t n, int32_t *q,
+                             int32_t *cnt3, int32_t *stats, int32_t *gmin2, int32_t *stop) {
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int32_t s = srcs[i];
+    if (sssp) {
+      vd.dist[s] = 0;
+    } else {
+      vd.parent[s] = s;
+      vd.depth[s] = 0;
+    }
+    q[i] = s;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    cnt3[0] = n;
+    cnt3[1] = 0;
+    cnt3[2] = 0;
+    stats[0] = 0;
+    stats[1] = 0;
+    gmin2[0] = INT_MAX;
+    gmin2[1] = INT_MAX;
+    *stop = 0;
+  }
+}
+
+gg_status fused_multi_enqueue(gg_graph *g, cudaStream_t st, bool sssp, const int32_t *dsrc, int32_t n,
+                              int32_t delta, int32_t *parent, int32_t *out) {
+  gg_frontier *f = g->app_frontier;
+  if (!f) return set_error(GG_ERR_STATE, "multi-source run: the graph's frontier is not created");
+  VData vd{};
+  if (sssp) {
+    vd.dist = out;
+  } else {
+    vd.parent = parent;
+    vd.depth = out;
+  }
+  vd.src = -1;
+  FusedArgs a = make_args(g, f, vd);
+  a.delta = delta;
+  const int cta = 512;
+  const size_t smem = twce_smem_bytes(cta);
+  const void *kernel = sssp ? (const void *)k_sssp_fused<GG_LB_TWCE> : (const void *)k_bfs_fused<GG_LB_TWCE>;
+  int per_sm = 0;
+  GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, cta, smem));
+  if (per_sm < 1) return set_error(GG_ERR_UNSUPPORTED, "fused kernel does not fit on an SM");
+  note_launch();
+  k_multi_reset<<<g->sm_count * 8, 256, 0, st>>>(vd, sssp, g->csr.V);
+  note_launch();
+  k_multi_seed<<<std::max(1, std::min(ceil_div(n, 256), g->sm_count)), 256, 0, st>>>(
+      vd, sssp, dsrc, n, a.q0, a.cnt3, a.stats, a.gmin2, a.stop);
+  GG_CUDA(cudaMemsetAsync(g->d_bar, 0, sizeof(uint32_t) * 2, st));
+  void *args[] = {&a};
+  note_launch();
+  GG_CUDA(cudaLaunchCooperativeKernel(kernel, per_sm * g->sm_count, cta, args, smem, st));
+  return GG_OK;
+}
+
 // A barrier that waits for one block more than were launched: it can only end
 // by its time limit.
 __global__ void k_barrier_never(uint32_t *bar, int32_t *err, uint64_t timeout_ns) {

@@ -543,7 +543,8 @@ def sssp_batch(g: GraphT, sources, delta: int, out=None):
 class BatchPlan:
     """A batched BFS ("bfs"), SSSP ("sssp") or BC ("bc") captured into a CUDA
     graph once and replayed by run().  `out` is a CUDA tensor of shape
-    [nsrc, V]: int32 for BFS and SSSP, float32 for BC."""
+    [nsrc, V]: int32 for BFS and SSSP, float32 for BC.  "bfs_multi" /
+    "sssp_multi" capture one multi-source traversal into `out` of shape [V]."""
 
     def __init__(self, g: GraphT, app: str, sources, out, delta: int = 32):
         self.g = g
@@ -570,7 +571,7 @@ class BatchPlan:
             pass
 
 
-BATCH_APPS = {"bfs": 0, "sssp": 1, "bc": 2}
+BATCH_APPS = {"bfs": 0, "sssp": 1, "bc": 2, "bfs_multi": 3, "sssp_multi": 4}
 
 
 def set_batch_tuning(g: GraphT, app: str, blocks_per_sm: int = 0, chunk: int = 0,

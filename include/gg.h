@@ -402,9 +402,14 @@ gg_status gg_bc_batch(gg_graph *g, const int32_t *sources, int32_t nsrc,
  * once into a CUDA graph (every persistent launch of every group of sources)
  * and replayed with one graph launch per run.  `out` must be device memory:
  * nsrc*V int32 (BFS depths, SSSP distances) or float (BC dependencies).  The
- * plan copies the sources and owns its device state; delta is used by SSSP. */
+ * plan copies the sources and owns its device state; delta is used by SSSP.
+ * GG_BATCH_BFS_MULTI / GG_BATCH_SSSP_MULTI capture one multi-source traversal
+ * (gg_bfs_multi / gg_sssp_multi with the TWCE fused loop; one persistent
+ * launch) writing V int32 into `out`: over a disjoint union of graphs with one
+ * source per part, every part's own BFS / SSSP. */
 typedef struct gg_batch_plan gg_batch_plan;
-enum { GG_BATCH_BFS = 0, GG_BATCH_SSSP = 1, GG_BATCH_BC = 2 };
+enum { GG_BATCH_BFS = 0, GG_BATCH_SSSP = 1, GG_BATCH_BC = 2,
+       GG_BATCH_BFS_MULTI = 3, GG_BATCH_SSSP_MULTI = 4 };
 gg_status gg_batch_plan_create(gg_graph *g, int32_t app, const int32_t *sources,
                                int32_t nsrc, int32_t delta, void *out,
                                gg_batch_plan **plan);

@@ -244,3 +244,30 @@ def test_autotune_sets_the_fastest_candidate(app):
                 np.testing.assert_array_equal(dist[i], oracle.sssp_dijkstra(off, dst, w, int(srcs[i])))
     finally:
         set_batch_tuning(g, app)
+
+
+@pytest.mark.parametrize("app", ["bfs", "sssp"])
+def test_multigraph_plan_is_one_captured_launch(app):
+    """The mix of uneven graphs as one multi-source traversal captured into a
+    CUDA graph: replays equal the per-graph oracle results."""
+    import torch
+    from easy_graphit_gb300 import BatchPlan
+    parts = [HostGraph.rmat(9 + i % 4, 4 + 5 * i, seed=300 + i) if i % 3 else HostGraph.grid(20 + i, 20 + i, seed=400 + i)
+             for i in range(9)]
+    local = [int(p.pick_sources(1, seed=i)[0]) for i, p in enumerate(parts)]
+    hg, offs = HostGraph.union(parts)
+    g = GraphT(hg)
+    srcs = np.array([offs[i] + s for i, s in enumerate(local)], dtype=np.int32)
+    out = torch.full((hg.num_vertices,), -7, dtype=torch.int32, device="cuda")
+    plan = BatchPlan(g, app + "_multi", srcs, out, delta=16)
+    for _ in range(2):
+        st = plan.run()
+        assert st["launches"] >= 1 and st["iterations"] > 0
+        got = out.cpu().numpy()
+        for i, (p, s) in enumerate(zip(parts, local)):
+            off, dst, w = np.array(p.offsets), np.array(p.dst), np.array(p.weights)
+            ref = oracle.bfs(off, dst, s) if app == "bfs" else oracle.sssp_dijkstra(off, dst, w, s)
+            np.testing.assert_array_equal(got[offs[i]:offs[i + 1]], ref)
+        out.fill_(-7)
+    plan.close()
+    g.close()

@@ -156,6 +156,18 @@ def test_mix_of_64_uneven_graphs(app):
     assert (spec[:, 0] == 1).any() and (spec[:, 0] == 0).any()
     local = [int(p.pick_sources(1, seed=i)[0]) for i, p in enumerate(parts)]
     res, st = multigraph_batch(parts, app, local, delta=32)
+    # the same traversal captured into a CUDA graph (one persistent launch per replay)
+    import torch
+    from easy_graphit_gb300 import BatchPlan
+    hg, offs = HostGraph.union(parts)
+    g = GraphT(hg)
+    srcs = np.array([offs[i] + s for i, s in enumerate(local)], dtype=np.int32)
+    out = torch.empty((hg.num_vertices,), dtype=torch.int32, device="cuda")
+    plan = BatchPlan(g, app + "_multi", srcs, out, delta=32)
+    plan.run()
+    np.testing.assert_array_equal(out.cpu().numpy(), np.concatenate(res))
+    plan.close()
+    g.close()
     for i, (p, s, r) in enumerate(zip(parts, local, res)):
         off, dst, w = np.array(p.offsets), np.array(p.dst), np.array(p.weights)
         if app == "bfs":
