@@ -48,6 +48,8 @@ struct BsState {
   uint32_t *fr, *nacc, *far;  // [V] masks
   int32_t *qstamp;            // [V]
   int64_t *q[2];              // queue entries (u << 32 | chunk)
+  int64_t *hq[2];             // further chunks of the queue's high-degree vertices
+  int32_t *hcnt;              // [3] their counts (rotating)
   int64_t qcap;
   int32_t *fl[2];             // far lists
   int32_t *cnt;               // [0..2] queue counts (rotating), [3..4] far counts, [5..7] active masks

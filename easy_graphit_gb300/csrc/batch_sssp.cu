@@ -65,6 +65,16 @@ __device__ __forceinline__ int32_t bs_batch(int64_t n, int64_t nwarps) {
   return (int32_t)(per < 1 ? 1 : (per > 32 ? 32 : per));
 }
 
+// Relax-time queueing: one entry (chunk 0) per vertex, without the degree
+// lookup; the publish phase adds the further chunks of high-degree vertices.
+__device__ __forceinline__ void bs_enqueue_first(const BsState &S, int64_t *q, int32_t *qcnt, int32_t v) {
+  const int32_t pos = agg_inc(qcnt);
+  if (pos < S.qcap)
+    q[pos] = (int64_t)v << 32;
+  else
+    atomicOr(S.err, DEV_ERR_OVERFLOW);
+}
+
 __device__ __forceinline__ void bs_far_push(const BsState &S, int p, int32_t v) {
   const int32_t pos = agg_inc(S.cnt + 3 + p);
   if (pos < S.V)
@@ -79,7 +89,8 @@ __device__ __forceinline__ void bs_far_push(const BsState &S, int p, int32_t v) 
 // the per-entry load chains overlap.  Entries active for at most ep_max sources have their edges
 // flattened over the lanes (lane = edge, looping over the entry's sources);
 // the others run one at a time with lane = source.
-__device__ __forceinline__ void bs_relax(const BsState &S, int64_t n, const int64_t *qi, int64_t *qo,
+__device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64_t n, const int64_t *qi,
+                                         const int64_t *hqi, int64_t *qo,
                                          int32_t *qcnt_out, int32_t cut, const int32_t *s_cut, int p,
                                          int32_t it, int32_t *wctr, int64_t nwarps) {
   const int32_t lane = threadIdx.x & 31;
@@ -97,7 +108,7 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n, const int6
     int32_t u = 0, b = 0, cnt = 0;
     uint32_t m = 0;
     if (lane < B && e < n) {
-      const int64_t item = __ldcg(qi + e);
+      const int64_t item = e < n_main ? __ldcg(qi + e) : __ldcg(hqi + (e - n_main));
       u = (int32_t)(item >> 32);
       const int32_t c = (int32_t)(item & 0xffffffff);
       m = __ldcg(S.fr + u);
@@ -159,7 +170,7 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n, const int6
                 if (np < s_cut[s]) {
                   if (atomicOr(S.nacc + v, 1u << s) == 0u) {
                     S.qstamp[v] = it;
-                    bs_enqueue(S, qo, qcnt_out, v);
+                    bs_enqueue_first(S, qo, qcnt_out, v);
                   }
                 } else if (atomicOr(S.far + v, 1u << s) == 0u) {
                   bs_far_push(S, p, v);
@@ -225,7 +236,7 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n, const int6
           }
           if (my_nb && atomicOr(S.nacc + my_v, my_nb) == 0u) {
             S.qstamp[my_v] = it;
-            bs_enqueue(S, qo, qcnt_out, my_v);
+            bs_enqueue_first(S, qo, qcnt_out, my_v);
           }
           if (my_fb && atomicOr(S.far + my_v, my_fb) == 0u) bs_far_push(S, p, my_v);
         }
@@ -256,7 +267,9 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
       S.cnt[(it + 1) % 3] = 0;
       S.cnt[5 + (it + 1) % 3] = 0;
       S.wctr[(it + 1) % 3] = 0;
+      S.hcnt[(it + 1) % 3] = 0;
     }
+    const int32_t nh = *(volatile int32_t *)(S.hcnt + (it - 1) % 3);
     const int p = (int)(adv & 1);
     // ---- relax
     {
@@ -265,7 +278,8 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
       const int32_t cut = cl > INT_MAX ? INT_MAX : (int32_t)cl;
       if (threadIdx.x < kLanes) s_cut[threadIdx.x] = cut;
       __syncthreads();
-      bs_relax(S, n, S.q[in], S.q[in ^ 1], qcnt_out, cut, s_cut, p, it, S.wctr + it % 3, nwarps);
+      bs_relax(S, n, (int64_t)n + nh, S.q[in], S.hq[in], S.q[in ^ 1], qcnt_out, cut, s_cut, p, it, S.wctr + it % 3,
+               nwarps);
     }
     if (!grid_barrier(S.bar, gridDim.x, S.err, S.timeout_ns)) break;
     // ---- publish near masks of the queued vertices; OR them into the active set
@@ -282,6 +296,15 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
             x = __ldcg(S.nacc + v);
             S.nacc[v] = 0;
             S.fr[v] = x;
+            const int32_t nch = ceil_div(S.off[v + 1] - S.off[v], S.chunk);
+            if (nch > 1 && x) {  // chunks 1 .. nch-1 of a high-degree vertex queued by the relax
+              const int32_t pos = atomicAdd(S.hcnt + it % 3, nch - 1);
+              if ((int64_t)pos + nch - 1 > S.qcap) {
+                atomicOr(S.err, DEV_ERR_OVERFLOW);
+              } else {
+                for (int32_t c = 1; c < nch; ++c) S.hq[in ^ 1][pos + c - 1] = ((int64_t)v << 32) | (uint32_t)c;
+              }
+            }
           }
         }
         act |= x;
@@ -458,7 +481,10 @@ __global__ void k_bsssp_init(BsState S, const int32_t *__restrict__ srcs, int32_
 __global__ void k_bsssp_seed(BsState S, const int32_t *__restrict__ srcs, int32_t nsrc) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   for (int32_t i = 0; i < 8; ++i) S.cnt[i] = 0;
-  for (int32_t i = 0; i < 3; ++i) S.wctr[i] = 0;
+  for (int32_t i = 0; i < 3; ++i) {
+    S.wctr[i] = 0;
+    S.hcnt[i] = 0;
+  }
   *S.stop = 0;
   for (int32_t s = 0; s < kLanes; ++s) {
     S.cur[s] = s < nsrc ? 0 : INT_MAX;
@@ -508,7 +534,7 @@ gg_status bsssp_buffers(gg_graph *g, int32_t nsrc, bool owned, BsBuffers *b) {
   b->qcap = (int64_t)V + E / kMinChunk + 64;  // any tuning's chunk fits
   b->owned = owned;
   const size_t sz[6] = {sizeof(int32_t) * (size_t)V * kLanes, sizeof(uint32_t) * 3 * (size_t)V,
-                        sizeof(int32_t) * (3 * (size_t)V + 256), sizeof(int64_t) * 2 * (size_t)b->qcap,
+                        sizeof(int32_t) * (3 * (size_t)V + 256), sizeof(int64_t) * 4 * (size_t)b->qcap,
                         sizeof(int32_t) * (size_t)std::min(nsrc, kLanes) * V,
                         sizeof(int32_t) * (size_t)std::max(nsrc, kLanes)};
   void **ptr[6] = {(void **)&b->dist, (void **)&b->masks, (void **)&b->ints, (void **)&b->queues,
@@ -541,6 +567,9 @@ BsState bsssp_state(gg_graph *g, const BsBuffers &b, int32_t delta) {
   S.wctr = hdr + 144;       // 3
   S.q[0] = b.queues;
   S.q[1] = b.queues + b.qcap;
+  S.hq[0] = b.queues + 2 * b.qcap;
+  S.hq[1] = b.queues + 3 * b.qcap;
+  S.hcnt = hdr + 150;       // 3
   S.qcap = b.qcap;
   S.off = g->rel->g.off;  // the degree-ordered copy (bsssp_buffers built it)
   S.dst = g->rel->g.dst;
