@@ -25,7 +25,8 @@ struct GraphStore {
 // The graph renumbered by descending in-degree class (relabel.cu), with the
 // maps old -> new (perm) and new -> old (inv).
 struct Relabeled {
-  GraphStore g;
+  GraphStore g;                      // renumbered CSR
+  GraphStore csc;                    // renumbered in-lists (directed graphs, built on demand)
   int32_t *perm = nullptr, *inv = nullptr;
 };
 
@@ -123,6 +124,7 @@ int resident_grid(const void *kernel, int cta, size_t smem, int sm_count);
 
 // ---- relabel.cu
 gg_status ensure_relabel(gg_graph *g);
+gg_status ensure_relabel_csc(gg_graph *g);  // rel->csc for directed graphs (after ensure_relabel)
 void free_relabel(gg_graph *g);
 
 // ---- pagerank.cu

@@ -10,7 +10,10 @@
 // iteration's contributions go to the other half of a double buffer.
 //
 // The gathers are latency-bound (contrib is L2-resident, its reads random), so
-// every lane keeps four independent contrib loads in flight.
+// every lane keeps four independent contrib loads in flight, and the iteration
+// runs on the degree-ordered copy of the graph (relabel.cu): the contributions
+// of the high-degree vertices, read by most in-edges, share cache lines.  Ranks
+// come back to the caller's ids at the end.
 #include <algorithm>
 #include <vector>
 
@@ -125,6 +128,12 @@ __global__ void k_pr_bin(const int32_t *__restrict__ toff, int32_t V, int32_t *_
   }
 }
 
+__global__ void k_pr_unperm(const float *__restrict__ rank_new, const int32_t *__restrict__ perm, int32_t V,
+                            float *__restrict__ rank) {
+  for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+    rank[v] = rank_new[perm[v]];
+}
+
 __global__ void k_pr_init(const int32_t *__restrict__ off, int32_t V, float inv_v, float *rank, float *contrib) {
   for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
     rank[v] = inv_v;  // pr.cpp:43-46
@@ -212,20 +221,23 @@ static gg_status pr_plan(gg_graph *g, const GraphStore &t, PrPlan *P) {
   return GG_OK;
 }
 
-gg_status pagerank_pull_twc(gg_graph *g, int32_t iters, float damping, float *rank, float *contrib2) {
-  GG_TRY(ensure_transpose(g));
+gg_status pagerank_pull_twc(gg_graph *g, int32_t iters, float damping, float *rank_out, float *contrib2) {
+  GG_TRY(ensure_relabel(g));
+  GG_TRY(ensure_relabel_csc(g));
   const int32_t V = g->csr.V;
-  const GraphStore &t = g->csc ? *g->csc : g->csr;
+  const GraphStore &t = g->symmetric ? g->rel->g : g->rel->csc;  // in-lists in new ids
+  float *rank = nullptr;  // ranks in new ids
+  GG_TRY(scratch_get_app(g, 4, sizeof(float) * std::max(V, 1), (void **)&rank));
   PrPlan P;
   GG_TRY(pr_plan(g, t, &P));
   cudaStream_t st = g->stream;
   const float inv_v = (float)(1.0 / V);
   note_launch();
-  k_pr_init<<<g->sm_count * 8, 256, 0, st>>>(g->csr.off, V, inv_v, rank, contrib2);
+  k_pr_init<<<g->sm_count * 8, 256, 0, st>>>(g->rel->g.off, V, inv_v, rank, contrib2);
   PrArgs a{};
   a.toff = t.off;
   a.tsrc = t.dst;
-  a.off = g->csr.off;
+  a.off = g->rel->g.off;  // out-degrees in new ids
   a.rank = rank;
   a.beta = (float)((1.0 - (double)damping) / V);  // pr.cpp:37
   a.damp = damping;
@@ -249,6 +261,8 @@ gg_status pagerank_pull_twc(gg_graph *g, int32_t iters, float damping, float *ra
                                                                                                nh, P.partial);
     }
   }
+  note_launch();
+  k_pr_unperm<<<g->sm_count * 8, 256, 0, st>>>(rank, g->rel->perm, V, rank_out);
   GG_CUDA(cudaGetLastError());
   return GG_OK;
 }

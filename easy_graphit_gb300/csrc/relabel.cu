@@ -150,11 +150,35 @@ gg_status ensure_relabel(gg_graph *g) {
   return GG_OK;
 }
 
+// The renumbered in-lists: row i holds the in-neighbours of inv[i], renamed.
+gg_status ensure_relabel_csc(gg_graph *g) {
+  if (!g->rel) return set_error(GG_ERR_STATE, "relabelled graph missing");
+  if (g->symmetric || g->rel->csc.off) return GG_OK;  // a symmetric graph's CSR is its CSC
+  GG_TRY(ensure_transpose(g));
+  cudaStream_t st = g->stream;
+  const GraphStore &t = *g->csc;
+  Relabeled &r = *g->rel;
+  const int32_t V = t.V;
+  int32_t *partial = nullptr;
+  GG_CUDA(cudaMallocAsync(&r.csc.off, sizeof(int32_t) * (V + 1), st));
+  GG_CUDA(cudaMallocAsync(&r.csc.dst, sizeof(int32_t) * std::max(t.E, 1), st));
+  GG_CUDA(cudaMallocAsync(&r.csc.w, sizeof(int32_t) * std::max(t.E, 1), st));
+  GG_CUDA(cudaMallocAsync(&partial, sizeof(int32_t) * scan_scratch_ints(V), st));
+  r.csc.V = V;
+  r.csc.E = t.E;
+  GG_CUDA(exclusive_scan(RlDegIn{t.off, r.inv}, V, r.csc.off, partial, st));
+  note_launch();
+  k_rl_lists<<<g->sm_count * 8, 256, 0, st>>>(t.off, t.dst, t.w, r.perm, r.inv, V, r.csc.off, r.csc.dst, r.csc.w);
+  GG_CUDA(cudaGetLastError());
+  cudaFreeAsync(partial, st);
+  return GG_OK;
+}
+
 void free_relabel(gg_graph *g) {
   if (!g->rel) return;
   cudaStream_t st = g->stream;
   for (void *p : {(void *)g->rel->perm, (void *)g->rel->inv, (void *)g->rel->g.off, (void *)g->rel->g.dst,
-                  (void *)g->rel->g.w})
+                  (void *)g->rel->g.w, (void *)g->rel->csc.off, (void *)g->rel->csc.dst, (void *)g->rel->csc.w})
     if (p) cudaFreeAsync(p, st);
   g->rel.reset();
 }
