@@ -401,7 +401,7 @@ def per_app(g, hg, off, dst, dev, stream):
     or static-gather path on the same graph, device-timed; outputs compared."""
     import torch
 
-    from easy_graphit_gb300 import (SimpleGPUSchedule as T, bc, bc_batch, bfs, bfs_batch,
+    from easy_graphit_gb300 import (SimpleGPUSchedule as T, bc, bc_batch, bfs, bfs_batch, cc,
                                     default_schedule, pagerank)
     E = hg.num_edges
     srcs = np.ascontiguousarray(hg.pick_sources(64, seed=27491095), dtype=np.int32)
@@ -436,6 +436,15 @@ def per_app(g, hg, off, dst, dev, stream):
                  "batched_gteps": st["edges_traversed"] / st["loop_ms"] / 1e6,
                  "rel_l1_batched_vs_plain": rel,
                  "plain_schedule": "PUSH TWCE fused (bc.cpp default); TEPS = 2 E_r / t"}
+    # CC: cc.cpp's EDGE_ONLY hook / pointer-jump rounds vs the fused union-find pass
+    sch, _ = default_schedule("cc")
+    cc(g, sch)
+    lab_r, st_r = cc(g, sch)
+    cc(g, sch, True)
+    lab_f, st_f = cc(g, sch, True)
+    res["cc"] = {"plain_gteps": E / st_r["device_ms"] / 1e6, "fused_gteps": E / st_f["device_ms"] / 1e6,
+                 "exact": bool(np.array_equal(lab_r, lab_f)), "plain_rounds": st_r["iterations"],
+                 "plain_schedule": "PUSH EDGE_ONLY rounds (cc.cpp default); TEPS = E / t (weak components)"}
     # PageRank: pr.cpp's PULL EDGE_ONLY blocked vs PULL TWC (static in-degree bins)
     sch, _ = default_schedule("pr")
     pagerank(g, 20, 0.85, sch)

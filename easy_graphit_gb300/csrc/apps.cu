@@ -453,6 +453,24 @@ gg_status gg_cc(gg_graph *g, const gg_app_schedule *s, int32_t *labels_out, gg_s
   if (st) *st = gg_stats{};
   int32_t *ids = nullptr, *updates = nullptr;
   GG_TRY(app_array(g, 0, V, &ids));
+  if (s->fuse && s->kind == GG_SCHED_SIMPLE) {
+    // the whole computation fused into one edge pass (cc_uf.cu): same labels
+    int32_t *parent = nullptr;
+    GG_TRY(app_array(g, 2, V, &parent));
+    Trial t(g);
+    GG_TRY(cc_union_find(g, ids, parent));
+    GG_TRY(t.stop(st));
+    GG_TRY(check_device_error(g, "cc"));
+    if (labels_out) GG_CUDA(cudaMemcpyAsync(labels_out, ids, sizeof(int32_t) * V, cudaMemcpyDefault, g->stream));
+    if (st) {
+      st->iterations = 1;
+      st->fused = 1;
+      st->vertices_reached = V;
+      st->edges_traversed = (int64_t)g->csr.E;
+    }
+    GG_CUDA(cudaStreamSynchronize(g->stream));
+    return GG_OK;
+  }
   GG_TRY(app_array(g, 1, 2, &updates));
   VData vd{};
   vd.ids = ids;

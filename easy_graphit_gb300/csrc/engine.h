@@ -122,6 +122,9 @@ gg_status scratch_get(gg_graph *g, int slot, size_t bytes, void **p);
 gg_status scratch_get_app(gg_graph *g, int slot, size_t bytes, void **p);
 int resident_grid(const void *kernel, int cta, size_t smem, int sm_count);
 
+// ---- cc_uf.cu
+gg_status cc_union_find(gg_graph *g, int32_t *labels, int32_t *parent);
+
 // ---- relabel.cu
 gg_status ensure_relabel(gg_graph *g);
 gg_status ensure_relabel_csc(gg_graph *g);  // rel->csc for directed graphs (after ensure_relabel)

@@ -497,11 +497,12 @@ def pagerank(g: GraphT, iters: int = 20, damping: float = 0.85, schedule=None):
     return rank, _stats(st)
 
 
-def cc(g: GraphT, schedule=None):
-    """apps/cc.cpp: returns (labels, stats); label = min vertex id of the component."""
+def cc(g: GraphT, schedule=None, fuse=None):
+    """apps/cc.cpp: returns (labels, stats); label = min vertex id of the component.
+    fuse=True runs the whole computation as one union-find pass (same labels)."""
     labels = np.empty(g.num_vertices, dtype=np.int32)
     st = L.gg_stats()
-    a = _resolve("cc", schedule, False)
+    a = _resolve("cc", schedule, fuse)
     call("gg_cc", g.handle, C.byref(a), _ptr(labels), C.byref(st))
     return labels, _stats(st)
 

@@ -317,7 +317,10 @@ gg_status gg_sssp(gg_graph *g, const gg_app_schedule *s, int32_t src,
 /* PageRank, `iters` iterations of pr.cpp:60-64; rank_out = old_rank. */
 gg_status gg_pagerank(gg_graph *g, const gg_app_schedule *s, int32_t iters,
                       float damping, float *rank_out, gg_stats *stats);
-/* Connected components (cc.cpp); labels_out[v] = min vertex id of v's component. */
+/* Connected components (cc.cpp); labels_out[v] = min vertex id of v's component.
+ * With s->fuse set (cc.cpp's main leaves it off) the hook / pointer-jump rounds
+ * are fused into one pass over the edges: a lock-free union-find whose roots
+ * are the smallest ids of their trees, giving the same labels. */
 gg_status gg_cc(gg_graph *g, const gg_app_schedule *s, int32_t *labels_out,
                 gg_stats *stats);
 /* Single-source betweenness dependencies (bc.cpp) from src. */

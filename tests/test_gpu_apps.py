@@ -293,3 +293,16 @@ def test_deterministic_outputs():
     d2, _ = sssp(g, s, 8)
     np.testing.assert_array_equal(d1, d2)
     assert rel_l1(r1, r2) < 1e-6
+
+
+@pytest.mark.parametrize("kind", ["sym12", "dir12", "sym16", "dir16", "grid"])
+def test_cc_fused_union_find_matches_the_rounds(kind):
+    """fuse = 1 runs CC as one union-find pass; labels equal cc.cpp's rounds
+    and the oracle's (minimum id per weakly connected component)."""
+    hg, g, (off, dst, _) = graph(kind)
+    sch, _ = default_schedule("cc")
+    fused, st = cc(g, sch, True)
+    rounds, _ = cc(g, sch)
+    np.testing.assert_array_equal(fused, oracle.cc(off, dst))
+    np.testing.assert_array_equal(fused, rounds)
+    assert st["fused"] == 1
