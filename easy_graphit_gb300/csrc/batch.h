@@ -17,6 +17,7 @@ inline gg_batch_tuning effective_tuning(const gg_graph *g, int32_t app, int fit)
   if (t.blocks_per_sm <= 0 || t.blocks_per_sm > fit) t.blocks_per_sm = fit;
   if (t.chunk <= 0) t.chunk = 256;
   if (t.edge_parallel_max == 0) t.edge_parallel_max = 6;
+  if (t.bottom_up_div == 0) t.bottom_up_div = 16;
   return t;
 }
 constexpr int32_t kMsBfsWidth = 64;  // sources per batched-BFS pass (mask bits)
@@ -87,17 +88,22 @@ gg_status bsssp_enqueue(gg_graph *g, cudaStream_t st, const BsState &S, const in
 
 // ----------------------------------------------------------- batched BFS
 struct MsBfsState {
-  uint64_t *seen, *acc, *fr;  // V each
-  int32_t *qstamp;            // V: last level v was queued at
-  int32_t *q0, *q1;           // V each
-  int32_t *cnt3;              // rotating counts
+  uint64_t *seen, *acc;       // V each
+  uint64_t *fr[3];            // frontier masks of level L in fr[L % 3]
+  unsigned long long *actm;   // [3] OR of level L's masks (sources still expanding)
+  int32_t *qstamp;            // V: last top-down level v was queued at
+  int32_t *q[3];              // queue of level L in q[L % 3]
+  int32_t *cnt4;              // [4] queue count of level L in cnt4[L % 4]
+  const int32_t *toff, *tsrc; // in-lists, for bottom-up levels
+  int32_t V;
+  int32_t bu_div;             // bottom-up when the frontier holds more than V / bu_div vertices (<= 0: never)
   int32_t *depth;             // [nsrc][V] (row-major per source)
   int64_t depth_stride;       // V
   int32_t nsrc;
   uint32_t *bar;
   int32_t *err;
   uint64_t timeout_ns;
-  int32_t *stats;             // [0] levels
+  int32_t *stats;             // [0] levels, [1] bottom-up levels
   int32_t *stop;
   uint64_t loop_limit_ns;
 };

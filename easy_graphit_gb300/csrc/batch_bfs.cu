@@ -1,13 +1,21 @@
 // Batched BFS: up to 64 sources per pass in one persistent kernel.
 //
 // Bit-parallel multi-source BFS: every vertex carries 64-bit masks -- `seen`
-// (sources that reached it), `acc` (sources reaching it this level) and `fr`
-// (sources for which it is on the current frontier).  One traversal of an edge
-// (u, v) serves every source at once: acc[v] |= fr[u] & ~seen[v].  A level ends
-// with a grid barrier, then the vertices touched this level publish their new
-// bits (fr = acc & ~seen, seen |= fr), write depth[s][v] = level for each new
-// bit, and form the next frontier.  Frontier vertices are load-balanced by the
-// TWCE device function of lb.cuh, so hubs are split across a warp or the CTA.
+// (sources that reached it), `acc` (sources reaching it this level) and the
+// level masks fr (sources for which it is on the level's frontier).  Levels run
+// top-down or bottom-up (direction optimisation, as bfs.cpp's hybrid schedule
+// does for one source, here for all sources at once):
+//  * top-down: one traversal of an edge (u, v) serves every source,
+//    acc[v] |= fr[u] & ~seen[v]; frontier vertices are load-balanced by the TWCE
+//    device function of lb.cuh; a publish phase then turns new bits into the
+//    next level's masks and depths;
+//  * bottom-up (frontier larger than V / bu_div): groups of 8 lanes take the
+//    vertices some still-expanding source has not reached and OR the level
+//    masks of their in-neighbours, 8 at a time, stopping as soon as every such
+//    source is found; no atomics.
+// Level masks rotate through three arrays and queues through three buffers:
+// the masks of level L-1 are cleared (from its queue) while level L publishes,
+// so a bottom-up scan never reads a stale mask.
 //
 // The result for each source equals an independent BFS (apps/bfs.cpp), because
 // a source's bit enters seen[v] exactly at the first level that reaches v.
@@ -18,90 +26,164 @@
 
 namespace gg {
 
+__device__ __forceinline__ uint64_t *ms_fr(const MsBfsState &st, int32_t level) {
+  const int32_t i = level % 3;
+  return i == 0 ? st.fr[0] : (i == 1 ? st.fr[1] : st.fr[2]);
+}
+__device__ __forceinline__ int32_t *ms_q(const MsBfsState &st, int32_t level) {
+  const int32_t i = level % 3;
+  return i == 0 ? st.q[0] : (i == 1 ? st.q[1] : st.q[2]);
+}
+
+// depth[s][v] = level for every bit s of nb, the bits split over `ways` lanes.
+__device__ __forceinline__ void ms_depths(const MsBfsState &st, int32_t v, uint64_t nb, int32_t level,
+                                          int32_t sub, int32_t ways) {
+  if (!st.depth) return;
+  for (uint64_t b = nb; b; b &= b - 1) {
+    const int32_t s = __ffsll((long long)b) - 1;
+    if (s % ways == sub) st.depth[(int64_t)s * st.depth_stride + v] = level;
+  }
+}
+
 __global__ void __launch_bounds__(512) k_msbfs(DGraph g, MsBfsState st) {
   extern __shared__ int4 smem[];
-  int32_t *qs[2] = {st.q0, st.q1};
-  int in = 0;
-  int64_t level = 1;
-  const int32_t stride = gridDim.x * blockDim.x;
+  __shared__ unsigned long long s_act;
+  const int32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int32_t nthreads = gridDim.x * blockDim.x;
+  const int32_t lane = threadIdx.x & 31;
   LoopClock clk;
   clk.start(st.loop_limit_ns);
-  for (;; ++level) {
-    const int32_t n = *(volatile int32_t *)(st.cnt3 + (level - 1) % 3);
+  int32_t L = 0, bu_levels = 0;
+  for (;; ++L) {
+    const int32_t n = *(volatile int32_t *)(st.cnt4 + (L & 3));
     if (n == 0 || stopped(st.stop, st.err)) break;
-    if (blockIdx.x == 0 && threadIdx.x == 0) st.cnt3[(level + 1) % 3] = 0;
-    // relax: acc[v] |= fr[u] & ~seen[v]
-    {
-      const Enum en{qs[in], nullptr, n};
-      const UMsBfs f{st.seen, st.fr, st.acc, st.qstamp, (int32_t)level};
+    if (tid == 0) {
+      st.cnt4[(L + 2) & 3] = 0;
+      st.actm[(L + 2) % 3] = 0ull;
+    }
+    if (threadIdx.x == 0) s_act = 0ull;
+    __syncthreads();
+    const bool bu = st.bu_div > 0 && (int64_t)n * st.bu_div > st.V;
+    const uint64_t *frc = ms_fr(st, L);
+    uint64_t *frn = ms_fr(st, L + 1);
+    int32_t *qn = ms_q(st, L + 1);
+    if (!bu) {
+      // top-down: acc[v] |= fr[u] & ~seen[v]; the first toucher queues v
+      const Enum en{ms_q(st, L), nullptr, n};
+      const UMsBfs f{st.seen, frc, st.acc, st.qstamp, L + 1};
       DOut out{};
       out.mode = OUT_SPARSE;
-      out.q = qs[in ^ 1];
-      out.cnt = st.cnt3 + level % 3;
-      out.cap = g.V;  // qstamp admits each vertex once per level
+      out.q = qn;
+      out.cnt = st.cnt4 + ((L + 1) & 3);
+      out.cap = st.V;  // qstamp admits each vertex once per level
       out.err = st.err;
       const int32_t nv = ceil_div(n, blockDim.x / kStage1);
       for (int32_t v = blockIdx.x; v < nv; v += gridDim.x)
         lb_twce<UMsBfs, true>(g, en, n, f, out, v, *reinterpret_cast<TwceSmem *>(smem));
+    } else {
+      // bottom-up: 8-lane groups over the vertices still wanted by some source
+      ++bu_levels;
+      const uint64_t act = *(volatile unsigned long long *)(st.actm + L % 3);
+      const int32_t sub = lane & 7;
+      const uint32_t gmask = 0xFFu << (lane & ~7);
+      for (int32_t v = tid >> 3; v < st.V; v += nthreads >> 3) {
+        const uint64_t sv = __ldcg(st.seen + v);
+        const uint64_t want = act & ~sv;
+        if (!want) continue;
+        const int32_t kb = __ldg(st.toff + v), ke = __ldg(st.toff + v + 1);
+        uint64_t found = 0;
+        for (int32_t k0 = kb; k0 < ke; k0 += 8) {
+          uint64_t m = 0;
+          if (k0 + sub < ke) m = __ldcg(frc + __ldg(st.tsrc + k0 + sub)) & want;
+          m |= __shfl_xor_sync(gmask, m, 1);
+          m |= __shfl_xor_sync(gmask, m, 2);
+          m |= __shfl_xor_sync(gmask, m, 4);
+          found |= m;
+          if (found == want) break;
+        }
+        if (found) {
+          if (sub == 0) {
+            st.seen[v] = sv | found;
+            frn[v] = found;
+            const int32_t pos = atomicAdd(st.cnt4 + ((L + 1) & 3), 1);
+            if (pos < st.V)
+              qn[pos] = v;
+            else
+              atomicOr(st.err, DEV_ERR_OVERFLOW);
+            atomicOr(&s_act, (unsigned long long)found);
+          }
+          ms_depths(st, v, found, L + 1, sub, 8);
+        }
+      }
     }
     if (!grid_barrier(st.bar, gridDim.x, st.err, st.timeout_ns)) break;
-    // publish: new bits become the next frontier masks
-    {
-      const int32_t m = *(volatile int32_t *)(st.cnt3 + level % 3);
-      const int32_t *q = qs[in ^ 1];
-      for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
-        const int32_t v = q[i];
+    // publish (top-down levels): new bits become the next level's masks
+    if (!bu) {
+      const int32_t m = min(*(volatile int32_t *)(st.cnt4 + ((L + 1) & 3)), st.V);
+      for (int32_t i = tid; i < m; i += nthreads) {
+        const int32_t v = __ldcg(qn + i);
         const uint64_t a = __ldcg(st.acc + v);
         const uint64_t sv = __ldcg(st.seen + v);
         const uint64_t nb = a & ~sv;
         st.seen[v] = sv | nb;
-        st.fr[v] = nb;
+        frn[v] = nb;
         st.acc[v] = 0;
-        if (st.depth) {
-          uint64_t b = nb;
-          while (b) {
-            const int s = __ffsll((long long)b) - 1;
-            b &= b - 1;
-            st.depth[(int64_t)s * st.depth_stride + v] = (int32_t)level;
-          }
-        }
+        atomicOr(&s_act, (unsigned long long)nb);
+        ms_depths(st, v, nb, L + 1, 0, 1);
       }
     }
+    // the masks of level L-1 are dead: clear them for the bottom-up scans
+    if (L >= 1) {
+      uint64_t *old = ms_fr(st, L - 1);
+      const int32_t *qo = ms_q(st, L - 1);
+      const int32_t m = min(*(volatile int32_t *)(st.cnt4 + ((L - 1) & 3)), st.V);
+      for (int32_t i = tid; i < m; i += nthreads) old[__ldcg(qo + i)] = 0ull;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_act) atomicOr(st.actm + (L + 1) % 3, s_act);
     clk.tick(st.stop);
     if (!grid_barrier(st.bar, gridDim.x, st.err, st.timeout_ns)) break;
-    in ^= 1;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) st.stats[0] = (int32_t)(level - 1);
+  if (tid == 0) {
+    st.stats[0] = L;
+    st.stats[1] = bu_levels;
+  }
 }
 
-// Initial state: masks cleared, depth rows -1, sources seeded.
-__global__ void k_msbfs_init(MsBfsState st, int32_t V, const int32_t *__restrict__ srcs) {
+// Initial state: masks cleared, depth rows -1.
+__global__ void k_msbfs_init(MsBfsState st) {
   const int64_t total = (int64_t)st.nsrc * st.depth_stride;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x)
     st.depth[i] = -1;
-  for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+  for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < st.V; v += gridDim.x * blockDim.x) {
     st.seen[v] = 0;
     st.acc[v] = 0;
-    st.fr[v] = 0;
+    st.fr[0][v] = 0;
+    st.fr[1][v] = 0;
+    st.fr[2][v] = 0;
     st.qstamp[v] = 0;
   }
 }
 
+// Sources seeded (one thread: sources are few; duplicates share a vertex).
 __global__ void k_msbfs_seed(MsBfsState st, const int32_t *__restrict__ srcs) {
-  // one thread: sources are few; duplicates share a vertex
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   int32_t n = 0;
+  unsigned long long all = 0;
   for (int32_t s = 0; s < st.nsrc; ++s) {
     const int32_t v = srcs[s];
-    if (!st.seen[v]) st.q0[n++] = v;
+    if (!st.seen[v]) st.q[0][n++] = v;
     st.seen[v] |= 1ull << s;
-    st.fr[v] |= 1ull << s;
+    st.fr[0][v] |= 1ull << s;
+    all |= 1ull << s;
     st.depth[(int64_t)s * st.depth_stride + v] = 0;
   }
-  st.cnt3[0] = n;
-  st.cnt3[1] = 0;
-  st.cnt3[2] = 0;
+  for (int i = 0; i < 4; ++i) st.cnt4[i] = 0;
+  st.cnt4[0] = n;
+  st.actm[0] = all;
+  st.actm[1] = 0;
+  st.actm[2] = 0;
   *st.stop = 0;
 }
 
@@ -113,9 +195,10 @@ MsBfsBuffers::~MsBfsBuffers() {
 }
 
 gg_status msbfs_buffers(gg_graph *g, int32_t nsrc, bool owned, MsBfsBuffers *b) {
+  GG_TRY(ensure_transpose(g));  // in-lists for the bottom-up levels
   const int32_t V = g->csr.V;
   b->owned = owned;
-  const size_t sz[3] = {sizeof(uint64_t) * 3 * (size_t)V, sizeof(int32_t) * (3 * (size_t)V + 64),
+  const size_t sz[3] = {sizeof(uint64_t) * (5 * (size_t)V + 8), sizeof(int32_t) * (4 * (size_t)V + 64),
                         sizeof(int32_t) * (size_t)std::max(nsrc, kMsBfsWidth)};
   void **ptr[3] = {(void **)&b->masks, (void **)&b->ints, (void **)&b->dsrc};
   for (int i = 0; i < 3; ++i) {
@@ -129,16 +212,23 @@ gg_status msbfs_buffers(gg_graph *g, int32_t nsrc, bool owned, MsBfsBuffers *b) 
 
 MsBfsState msbfs_state(gg_graph *g, const MsBfsBuffers &b, int32_t k, int32_t *depth_rows) {
   const int32_t V = g->csr.V;
+  const GraphStore &t = g->csc ? *g->csc : g->csr;
   MsBfsState S{};
   S.seen = b.masks;
   S.acc = b.masks + V;
-  S.fr = b.masks + 2 * (size_t)V;
+  for (int i = 0; i < 3; ++i) S.fr[i] = b.masks + (2 + i) * (size_t)V;
+  S.actm = reinterpret_cast<unsigned long long *>(b.masks + 5 * (size_t)V);
   S.qstamp = b.ints;
-  S.q0 = b.ints + V;
-  S.q1 = b.ints + 2 * (size_t)V;
-  S.cnt3 = b.ints + 3 * (size_t)V;
-  S.stats = b.ints + 3 * (size_t)V + 8;
-  S.stop = b.ints + 3 * (size_t)V + 12;
+  for (int i = 0; i < 3; ++i) S.q[i] = b.ints + (1 + i) * (size_t)V;
+  int32_t *hdr = b.ints + 4 * (size_t)V;
+  S.cnt4 = hdr;          // 4
+  S.stats = hdr + 8;     // 2
+  S.stop = hdr + 12;
+  S.toff = t.off;
+  S.tsrc = t.dst;
+  S.V = V;
+  const gg_batch_tuning tn = effective_tuning(g, GG_BATCH_BFS, 1);
+  S.bu_div = tn.bottom_up_div;
   S.loop_limit_ns = loop_timeout_ns();
   S.depth = depth_rows;
   S.depth_stride = V;
@@ -161,7 +251,7 @@ gg_status msbfs_enqueue(gg_graph *g, cudaStream_t st, const MsBfsState &S, const
   GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_msbfs, cta, smem));
   if (per_sm < 1) return set_error(GG_ERR_UNSUPPORTED, "batched BFS kernel does not fit an SM");
   note_launch();
-  k_msbfs_init<<<g->sm_count * 8, 256, 0, st>>>(S, g->csr.V, dsrc);
+  k_msbfs_init<<<g->sm_count * 8, 256, 0, st>>>(S);
   note_launch();
   k_msbfs_seed<<<1, 32, 0, st>>>(S, dsrc);
   GG_CUDA(cudaMemsetAsync(S.bar, 0, sizeof(uint32_t) * 2, st));

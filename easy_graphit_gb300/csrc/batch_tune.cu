@@ -15,6 +15,7 @@ bool valid_tuning(const gg_batch_tuning &t) {
   if (t.blocks_per_sm < 0 || t.blocks_per_sm > 64) return false;
   if (t.chunk != 0 && (t.chunk < kMinChunk || t.chunk > kMaxChunk || (t.chunk & (t.chunk - 1)))) return false;
   if (t.edge_parallel_max < -1 || t.edge_parallel_max > 32) return false;
+  if (t.bottom_up_div < -1 || t.bottom_up_div > 4096) return false;
   return true;
 }
 
@@ -74,8 +75,9 @@ gg_status gg_batch_set_tuning(gg_graph *g, int32_t app, const gg_batch_tuning *t
   GG_CHECK_ARG(g && t, "bad arguments");
   GG_CHECK_ARG(app >= GG_BATCH_BFS && app <= GG_BATCH_BC, "unknown batched app");
   if (!valid_tuning(*t))
-    return set_error(GG_ERR_INVALID, "tuning out of range (blocks_per_sm %d, chunk %d, edge_parallel_max %d)",
-                     t->blocks_per_sm, t->chunk, t->edge_parallel_max);
+    return set_error(GG_ERR_INVALID,
+                     "tuning out of range (blocks_per_sm %d, chunk %d, edge_parallel_max %d, bottom_up_div %d)",
+                     t->blocks_per_sm, t->chunk, t->edge_parallel_max, t->bottom_up_div);
   g->tuning[app] = *t;
   return GG_OK;
 }
@@ -153,7 +155,16 @@ gg_status gg_batch_autotune(gg_graph *g, int32_t app, const int32_t *sources, in
     }
     cur = win;
   }
-  // 3. edge-parallel threshold (SSSP)
+  // 3. bottom-up threshold (BFS)
+  if (app == GG_BATCH_BFS) {
+    for (int d : {-1, 4, 64, 256}) {
+      if (d == cur.bottom_up_div) continue;
+      gg_batch_tuning t = cur;
+      t.bottom_up_div = d;
+      GG_TRY(time_one(t));
+    }
+  }
+  // 4. edge-parallel threshold (SSSP)
   if (app == GG_BATCH_SSSP) {
     for (int e : {-1, 2, 12, 32}) {
       if (e == cur.edge_parallel_max) continue;

@@ -23,7 +23,8 @@ APPS = [("bfs", 64), ("sssp", 32), ("bc", 64)]
 def builtin_row(rows, fit):
     """The trial that ran the built-in shape (all CTAs that fit, chunk 256, threshold 6)."""
     for t, ms in rows:
-        if t["blocks_per_sm"] == fit and t["chunk"] in (0, 256) and t["edge_parallel_max"] in (0, 6):
+        if (t["blocks_per_sm"] == fit and t["chunk"] in (0, 256) and t["edge_parallel_max"] in (0, 6)
+                and t["bottom_up_div"] in (0, 16)):
             return ms
     return None
 
@@ -33,8 +34,8 @@ def main():
     ap.add_argument("--out", default=None)
     ap.add_argument("--delta", type=int, default=32)
     a = ap.parse_args()
-    lines = ["| graph | V | E | app | sources | CTAs/SM | chunk | edge-parallel max | tuned ms | built-in ms | trials |",
-             "|---|---|---|---|---|---|---|---|---|---|---|"]
+    lines = ["| graph | V | E | app | sources | CTAs/SM | chunk | edge-parallel max | bottom-up div | tuned ms | built-in ms | trials |",
+             "|---|---|---|---|---|---|---|---|---|---|---|---|"]
     t0 = time.time()
     for kind, size in SIZES:
         for app, nsrc in APPS:
@@ -50,7 +51,8 @@ def main():
             base_s = f"{base:.3f}" if base is not None else "-"
             lines.append(f"| {name} | {hg.num_vertices} | {hg.num_edges} | {app} | {nsrc} | {best['blocks_per_sm']} | "
                          f"{best['chunk'] if app != 'bfs' else '-'} | "
-                         f"{best['edge_parallel_max'] if app == 'sssp' else '-'} | {ms:.3f} | {base_s} | {len(rows)} |")
+                         f"{best['edge_parallel_max'] if app == 'sssp' else '-'} | "
+                         f"{best['bottom_up_div'] if app == 'bfs' else '-'} | {ms:.3f} | {base_s} | {len(rows)} |")
             print(lines[-1], flush=True)
             set_batch_tuning(g, app)
             g.close()

@@ -426,20 +426,25 @@ gg_status gg_batch_plan_destroy(gg_batch_plan *plan);
  *                     two in [32, 4096] (default 256);
  *  edge_parallel_max  batched SSSP: work items active for at most this many
  *                     sources map lanes to edges, the others lanes to sources
- *                     (default 6; -1 = never edge-parallel; at most 32).
+ *                     (default 6; -1 = never edge-parallel; at most 32);
+ *  bottom_up_div      batched BFS: a level whose frontier holds more than
+ *                     V / bottom_up_div vertices runs bottom-up over in-lists
+ *                     (default 16; -1 = always top-down; at most 4096).
  * The tuning of `app` (GG_BATCH_*) applies to the batched calls and to plans
  * created after it is set. */
 typedef struct gg_batch_tuning {
   int32_t blocks_per_sm;
   int32_t chunk;
   int32_t edge_parallel_max;
+  int32_t bottom_up_div;
 } gg_batch_tuning;
 gg_status gg_batch_set_tuning(gg_graph *g, int32_t app, const gg_batch_tuning *t);
 gg_status gg_batch_get_tuning(const gg_graph *g, int32_t app, gg_batch_tuning *t);
 /* Autotuner: times candidate launch shapes of `app` on the graph (one pass
  * over the first min(nsrc, pass width) sources per candidate, best of two
  * timed runs of the persistent kernel), by coordinate descent over
- * blocks_per_sm, then chunk, then edge_parallel_max; sets the fastest as the
+ * blocks_per_sm, then chunk (SSSP, BC), edge_parallel_max (SSSP) or
+ * bottom_up_div (BFS); sets the fastest as the
  * graph's tuning and returns it in *best.  Every trial goes to rows (at most
  * max_rows; *nrows = trials run).  delta is used by SSSP. */
 typedef struct gg_tune_row {

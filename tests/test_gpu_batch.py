@@ -31,10 +31,16 @@ def graph(kind):
 
 @pytest.mark.parametrize("kind", ["dir14", "sym14", "grid"])
 @pytest.mark.parametrize("nsrc", [1, 5, 64, 100])
-def test_bfs_batch(kind, nsrc):
+@pytest.mark.parametrize("bottom_up", [0, -1, 4096])
+def test_bfs_batch(kind, nsrc, bottom_up):
+    from easy_graphit_gb300 import set_batch_tuning
     hg, g, (off, dst, _) = graph(kind)
     srcs = hg.pick_sources(nsrc, seed=11)
-    depth, st = bfs_batch(g, srcs)
+    set_batch_tuning(g, "bfs", bottom_up_div=bottom_up)
+    try:
+        depth, st = bfs_batch(g, srcs)
+    finally:
+        set_batch_tuning(g, "bfs")
     for i, s in enumerate(srcs):
         np.testing.assert_array_equal(depth[i], oracle.bfs(off, dst, int(s)), err_msg=f"source {s}")
 
@@ -196,7 +202,9 @@ def test_batch_plan_bc_replay():
 # ------------------------------------------------------------- launch tuning
 @pytest.mark.parametrize("tuning", [dict(blocks_per_sm=1), dict(chunk=32), dict(chunk=4096),
                                     dict(edge_parallel_max=-1), dict(edge_parallel_max=32),
-                                    dict(blocks_per_sm=2, chunk=64, edge_parallel_max=2)])
+                                    dict(blocks_per_sm=2, chunk=64, edge_parallel_max=2),
+                                    dict(bottom_up_div=-1), dict(bottom_up_div=4096),
+                                    dict(bottom_up_div=2, blocks_per_sm=1)])
 def test_batched_results_do_not_depend_on_tuning(tuning):
     from easy_graphit_gb300 import bc_batch, set_batch_tuning
     from tests.conftest import rel_l1
@@ -223,7 +231,7 @@ def test_invalid_tuning_is_rejected():
     from easy_graphit_gb300 import set_batch_tuning
     hg, g, _ = graph("dir14")
     for bad in (dict(chunk=48), dict(chunk=16), dict(chunk=8192), dict(edge_parallel_max=33),
-                dict(blocks_per_sm=-1)):
+                dict(blocks_per_sm=-1), dict(bottom_up_div=5000), dict(bottom_up_div=-2)):
         with pytest.raises(Exception, match="out of range"):
             set_batch_tuning(g, "sssp", **bad)
 
