@@ -113,6 +113,8 @@ gg_status edgeset_apply_impl(gg_graph *g, const gg_schedule *s, int32_t udf, int
   }
   if (edge_only && s->edge_blocking == GG_BLOCKED)
     GG_TRY(ensure_blocked(g, L.pull && !g->symmetric, s->block_size, &gs));
+  else if (edge_only && gs == &g->csr)
+    GG_TRY(ensure_coo(g->csr, g->stream));  // EDGE_ONLY walks the COO source column
   L.g = gs->view();
   if (!edge_only) L.g.nbuckets = 0;
   const bool sparse_out = s->frontier_creation == GG_FC_SPARSE;

@@ -399,8 +399,7 @@ gg_status gg_graph_create(const int32_t *offsets, const int32_t *dst, const int3
   GG_CUDA(cudaEventCreate(&g->ev1));
   GG_CUDA(cudaEventCreate(&g->ev2));
   GG_CUDA(cudaEventCreate(&g->ev3));
-  GG_TRY(ensure_coo(s, st));
-  GG_CUDA(cudaStreamSynchronize(st));
+  GG_CUDA(cudaStreamSynchronize(st));  // the COO source column is built on first use (ensure_coo)
   *out = g.release();
   return GG_OK;
 }
