@@ -69,6 +69,7 @@ struct BsState {
   uint64_t loop_limit_ns;
   int32_t *wctr;              // [3] relax work counters (rotating)
   const int32_t *perm;        // original id -> id in the degree-ordered graph the kernel walks
+  int32_t scan_div;           // a relax over >= V/scan_div queue entries marks masks without queueing (<= 0: never)
 };
 
 // Device buffers of one batched-SSSP pass; `owned` buffers are freed with it,

@@ -23,6 +23,13 @@
 // lose one.  The first thread to set a near bit of v in an iteration (its
 // atomicOr on the near mask returns 0) queues v.
 //
+// A relax over a large queue (at least V/scan_div entries) does not decide
+// who queues: it ORs the near and far masks without reading them back, the
+// publish phase then queues every vertex with a near mask by one coalesced
+// scan over all V, and the next advance scans all V for far masks (rebuilding
+// the far list).  Small relaxes keep the queue-on-first-bit path, so graphs
+// with thousands of small iterations never pay a V-sized scan per iteration.
+//
 // Iteration: relax | barrier | publish near masks, collect the active sources |
 // barrier | [advance pass 1 (minima) | barrier | pass 2 (move/keep) | barrier].
 #include <cooperative_groups/scan.h>
@@ -40,6 +47,7 @@ constexpr int32_t kPrefetch = 8;  // distance lines in flight per warp
 // (edges per queue entry) and S.ep_max come from the graph's batch tuning.
 
 constexpr uint32_t kFull = 0xffffffffu;
+constexpr int32_t kBsScanDiv = 64;  // relaxes over >= V/64 entries mark masks without queueing
 
 // Queues v as ceil(deg/chunk) entries.  The threads of a warp that enqueue
 // together reserve their entries with one atomic (coalesced-group scan).
@@ -92,7 +100,7 @@ __device__ __forceinline__ void bs_far_push(const BsState &S, int p, int32_t v) 
 __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64_t n, const int64_t *qi,
                                          const int64_t *hqi, int64_t *qo,
                                          int32_t *qcnt_out, int32_t cut, const int32_t *s_cut, int p,
-                                         int32_t it, int32_t *wctr, int64_t nwarps) {
+                                         int32_t it, int32_t *wctr, int64_t nwarps, bool scan) {
   const int32_t lane = threadIdx.x & 31;
   for (;;) {
     int32_t e0 = 0, B = 1;
@@ -168,10 +176,14 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64
               if (np < dv[t]) {
                 atomicMin(S.dist + (int64_t)v * kLanes + s, np);
                 if (np < s_cut[s]) {
-                  if (atomicOr(S.nacc + v, 1u << s) == 0u) {
+                  if (scan) {
+                    atomicOr(S.nacc + v, 1u << s);
+                  } else if (atomicOr(S.nacc + v, 1u << s) == 0u) {
                     S.qstamp[v] = it;
                     bs_enqueue_first(S, qo, qcnt_out, v);
                   }
+                } else if (scan) {
+                  atomicOr(S.far + v, 1u << s);
                 } else if (atomicOr(S.far + v, 1u << s) == 0u) {
                   bs_far_push(S, p, v);
                 }
@@ -234,11 +246,16 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64
               my_fb = fb;
             }
           }
-          if (my_nb && atomicOr(S.nacc + my_v, my_nb) == 0u) {
-            S.qstamp[my_v] = it;
-            bs_enqueue_first(S, qo, qcnt_out, my_v);
+          if (scan) {
+            if (my_nb) atomicOr(S.nacc + my_v, my_nb);
+            if (my_fb) atomicOr(S.far + my_v, my_fb);
+          } else {
+            if (my_nb && atomicOr(S.nacc + my_v, my_nb) == 0u) {
+              S.qstamp[my_v] = it;
+              bs_enqueue_first(S, qo, qcnt_out, my_v);
+            }
+            if (my_fb && atomicOr(S.far + my_v, my_fb) == 0u) bs_far_push(S, p, my_v);
           }
-          if (my_fb && atomicOr(S.far + my_v, my_fb) == 0u) bs_far_push(S, p, my_v);
         }
       }
     }
@@ -257,6 +274,7 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
   int in = 0;
   int64_t adv = 0;
   int32_t it = 1;
+  bool fdirty = false;  // a relax since the last advance marked far masks without listing them
   LoopClock clk;
   clk.start(S.loop_limit_ns);
   for (;; ++it) {
@@ -270,6 +288,8 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
       S.hcnt[(it + 1) % 3] = 0;
     }
     const int32_t nh = *(volatile int32_t *)(S.hcnt + (it - 1) % 3);
+    const bool scan = S.scan_div > 0 && ((int64_t)n + nh) * S.scan_div >= S.V;
+    fdirty |= scan;
     const int p = (int)(adv & 1);
     // ---- relax
     {
@@ -279,11 +299,25 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
       if (threadIdx.x < kLanes) s_cut[threadIdx.x] = cut;
       __syncthreads();
       bs_relax(S, n, (int64_t)n + nh, S.q[in], S.hq[in], S.q[in ^ 1], qcnt_out, cut, s_cut, p, it, S.wctr + it % 3,
-               nwarps);
+               nwarps, scan);
     }
     if (!grid_barrier(S.bar, gridDim.x, S.err, S.timeout_ns)) break;
     // ---- publish near masks of the queued vertices; OR them into the active set
-    {
+    if (scan) {  // queue every vertex with a near mask, all its chunks
+      uint32_t act = 0;
+      for (int64_t v = tid; v < S.V; v += tstride) {
+        const uint32_t x = __ldcg(S.nacc + v);
+        if (x) {
+          S.nacc[v] = 0;
+          S.fr[v] = x;
+          S.qstamp[v] = it;
+          bs_enqueue(S, S.q[in ^ 1], qcnt_out, (int32_t)v);
+          act |= x;
+        }
+      }
+      act = __reduce_or_sync(kFull, act);
+      if (lane == 0 && act) atomicOr(reinterpret_cast<uint32_t *>(S.cnt + 5 + it % 3), act);
+    } else {
       const int32_t mq = *(volatile int32_t *)qcnt_out;
       const int64_t *qo = S.q[in ^ 1];
       uint32_t act = 0;
@@ -323,7 +357,10 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
     const uint32_t active = (uint32_t)*(volatile int32_t *)(S.cnt + 5 + it % 3);
     const uint32_t A = unfinished & ~active;
     if (A) {
-      const int32_t fcount = min(*(volatile int32_t *)(S.cnt + 3 + p), S.V);
+      // after a scanning relax the far list misses vertices: walk all V instead
+      const bool fscan = fdirty;
+      fdirty = false;
+      const int32_t fcount = fscan ? S.V : min(*(volatile int32_t *)(S.cnt + 3 + p), S.V);
       const int32_t *fla = S.fl[p];
       const int32_t curl = __ldcg(S.cur + p * kLanes + lane);
       const int64_t window = (int64_t)curl + S.delta;
@@ -342,7 +379,7 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
         int32_t vl = 0;
         uint32_t fml = 0;
         if (lane < FB && e < fcount) {
-          vl = __ldcg(fla + e);
+          vl = fscan ? (int32_t)e : __ldcg(fla + e);
           fml = __ldcg(S.far + vl) & A;
         }
         uint32_t want = __ballot_sync(kFull, fml != 0u);
@@ -389,7 +426,7 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
         int32_t vl = 0;
         uint32_t fml = 0;
         if (mine) {
-          vl = __ldcg(fla + e);
+          vl = fscan ? (int32_t)e : __ldcg(fla + e);
           fml = __ldcg(S.far + vl);
         }
         uint32_t rem = fml & ~A;  // far bits of sources that do not advance stay
@@ -580,6 +617,7 @@ BsState bsssp_state(gg_graph *g, const BsBuffers &b, int32_t delta) {
   const gg_batch_tuning t = effective_tuning(g, GG_BATCH_SSSP, 1);
   S.chunk = t.chunk;
   S.ep_max = t.edge_parallel_max;
+  S.scan_div = kBsScanDiv;
   S.bar = g->d_bar;
   S.err = g->d_err;
   S.timeout_ns = barrier_timeout_ns();
