@@ -83,6 +83,65 @@ __device__ __forceinline__ void bs_enqueue_first(const BsState &S, int64_t *q, i
     atomicOr(S.err, DEV_ERR_OVERFLOW);
 }
 
+// Appends of a warp to a global list (queue or far list), collected in a
+// shared-memory buffer of kStage entries and written out with one atomicAdd
+// on the list's counter per kStage entries instead of one per warp step: the
+// scans over all V append from every warp, and one counter taking an atomic
+// from every warp step serialises.  The whole warp calls push() and flush().
+constexpr int32_t kStage = 128;
+
+template <typename T>
+struct WarpStage {
+  T *buf;     // kStage entries of this warp (shared memory)
+  T *list;    // the global list
+  int32_t *cnt;
+  int64_t cap;
+  int32_t n;  // staged entries (warp-uniform)
+
+  __device__ __forceinline__ void flush(int32_t *err) {
+    if (n == 0) return;
+    const int32_t lane = threadIdx.x & 31;
+    int32_t base = 0;
+    if (lane == 0) base = atomicAdd(cnt, n);
+    base = __shfl_sync(kFull, base, 0);
+    for (int32_t i = lane; i < n; i += 32) {
+      const int64_t pos = (int64_t)base + i;
+      if (pos < cap)
+        list[pos] = buf[i];
+      else
+        atomicOr(err, DEV_ERR_OVERFLOW);
+    }
+    __syncwarp();
+    n = 0;
+  }
+  __device__ __forceinline__ void push(bool app, T val, int32_t *err) {
+    const uint32_t am = __ballot_sync(kFull, app);
+    if (!am) return;
+    const int32_t k = __popc(am);
+    if (n + k > kStage) flush(err);
+    const int32_t lane = threadIdx.x & 31;
+    if (app) buf[n + __popc(am & ((1u << lane) - 1u))] = val;
+    __syncwarp();
+    n += k;
+  }
+};
+
+// Advances of at most kAdvFew sources walk the far entries with lane = entry:
+// lane l loads the distances of its entry for every advancing source with a
+// far bit there, all at once (instead of 4 entries at a time, lane = source).
+constexpr int32_t kAdvFew = 8;
+
+// ds[k] = dist[v][k-th source of A] where fa has that source's bit, else INT_MAX.
+__device__ __forceinline__ void bs_far_loads(const BsState &S, int32_t v, uint32_t fa, uint32_t A, int32_t nA,
+                                             int32_t (&ds)[kAdvFew]) {
+#pragma unroll
+  for (int32_t k = 0; k < kAdvFew; ++k) {
+    const int32_t s = A ? __ffs(A) - 1 : 0;
+    A &= A - 1;
+    ds[k] = (k < nA && ((fa >> s) & 1u)) ? __ldcg(S.dist + (int64_t)v * kLanes + s) : INT_MAX;
+  }
+}
+
 __device__ __forceinline__ void bs_far_push(const BsState &S, int p, int32_t v) {
   const int32_t pos = agg_inc(S.cnt + 3 + p);
   if (pos < S.V)
@@ -265,6 +324,8 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64
 __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
   __shared__ int32_t red[256 / 32][kLanes];
   __shared__ int32_t s_cut[kLanes];
+  __shared__ int64_t s_stq[256 / 32][kStage];  // staged queue entries per warp
+  __shared__ int32_t s_stl[256 / 32][kStage];  // staged far-list entries per warp
   const int32_t lane = threadIdx.x & 31;
   const int32_t wib = threadIdx.x >> 5;
   const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -304,17 +365,23 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
     if (!grid_barrier(S.bar, gridDim.x, S.err, S.timeout_ns)) break;
     // ---- publish near masks of the queued vertices; OR them into the active set
     if (scan) {  // queue every vertex with a near mask, all its chunks
+      WarpStage<int64_t> stq{s_stq[wib], S.q[in ^ 1], qcnt_out, S.qcap, 0};
       uint32_t act = 0;
-      for (int64_t v = tid; v < S.V; v += tstride) {
-        const uint32_t x = __ldcg(S.nacc + v);
+      for (int64_t v0 = tid - lane; v0 < S.V; v0 += tstride) {
+        const int64_t v = v0 + lane;
+        const uint32_t x = v < S.V ? __ldcg(S.nacc + v) : 0u;
+        bool one = false;
         if (x) {
           S.nacc[v] = 0;
           S.fr[v] = x;
           S.qstamp[v] = it;
-          bs_enqueue(S, S.q[in ^ 1], qcnt_out, (int32_t)v);
           act |= x;
+          one = S.off[v + 1] - S.off[v] <= S.chunk;
+          if (!one) bs_enqueue(S, S.q[in ^ 1], qcnt_out, (int32_t)v);
         }
+        stq.push(one, v << 32, S.err);
       }
+      stq.flush(S.err);
       act = __reduce_or_sync(kFull, act);
       if (lane == 0 && act) atomicOr(reinterpret_cast<uint32_t *>(S.cnt + 5 + it % 3), act);
     } else {
@@ -359,7 +426,11 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
     if (A) {
       // after a scanning relax the far list misses vertices: walk all V instead
       const bool fscan = fdirty;
-      fdirty = false;
+      // A pass over all V rebuilds the far list only when the next relax is
+      // likely to queue (it is small); before a scanning relax the list would
+      // be stale again.  (The queue count is stable here: only pass 2 adds.)
+      const bool relist = !fscan || (int64_t)*(volatile int32_t *)qcnt_out * S.scan_div < S.V;
+      fdirty = !relist;
       const int32_t fcount = fscan ? S.V : min(*(volatile int32_t *)(S.cnt + 3 + p), S.V);
       const int32_t *fla = S.fl[p];
       const int32_t curl = __ldcg(S.cur + p * kLanes + lane);
@@ -371,7 +442,10 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
       }
       // pass 1: per-source minimum far priority at or above the window.
       // Lane l loads far entry l of the warp's 32; the distance lines of the
-      // entries with advancing sources are then loaded 4 at a time.
+      // entries with advancing sources are then loaded 4 at a time (or, for
+      // at most kAdvFew advancing sources, lane = entry).
+      const int32_t nA = __popc(A);
+      const bool few = nA <= kAdvFew;
       int32_t mn = INT_MAX;
       const int32_t FB = bs_batch(fcount, nwarps);
       for (int64_t e0 = gwarp * FB; e0 < fcount; e0 += nwarps * FB) {
@@ -381,6 +455,21 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
         if (lane < FB && e < fcount) {
           vl = fscan ? (int32_t)e : __ldcg(fla + e);
           fml = __ldcg(S.far + vl) & A;
+        }
+        if (few) {
+          int32_t ds[kAdvFew];
+          bs_far_loads(S, vl, fml, A, nA, ds);
+          uint32_t aa = A;
+#pragma unroll
+          for (int32_t k = 0; k < kAdvFew; ++k) {
+            if (k >= nA) break;  // warp-uniform
+            const int32_t s = __ffs(aa) - 1;
+            aa &= aa - 1;
+            const int64_t win = __shfl_sync(kFull, window, s);
+            const int32_t m = __reduce_min_sync(kFull, (int64_t)ds[k] >= win ? ds[k] : INT_MAX);
+            if (lane == s && m < mn) mn = m;
+          }
+          continue;
         }
         uint32_t want = __ballot_sync(kFull, fml != 0u);
         while (want) {
@@ -420,6 +509,8 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
       const int32_t newcur = adv_l ? gm : curl;
       const int64_t hi = (int64_t)newcur + S.delta;
       int64_t *qo = S.q[in ^ 1];
+      WarpStage<int64_t> stq{s_stq[wib], qo, qcnt_out, S.qcap, 0};
+      WarpStage<int32_t> stl{s_stl[wib], S.fl[p ^ 1], S.cnt + 3 + (p ^ 1), S.V, 0};
       for (int64_t e0 = gwarp * FB; e0 < fcount; e0 += nwarps * FB) {
         const int64_t e = e0 + lane;
         const bool mine = lane < FB && e < fcount;
@@ -431,7 +522,28 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
         }
         uint32_t rem = fml & ~A;  // far bits of sources that do not advance stay
         uint32_t mv = 0;
-        uint32_t todo = __ballot_sync(kFull, (fml & A) != 0u);
+        if (few) {
+          const uint32_t fa = fml & A;
+          int32_t ds[kAdvFew];
+          bs_far_loads(S, vl, fa, A, nA, ds);
+          uint32_t aa = A;
+#pragma unroll
+          for (int32_t k = 0; k < kAdvFew; ++k) {
+            if (k >= nA) break;  // warp-uniform
+            const int32_t s = __ffs(aa) - 1;
+            aa &= aa - 1;
+            const int64_t win = __shfl_sync(kFull, window, s);
+            const int64_t his = __shfl_sync(kFull, hi, s);
+            const int32_t ncs = __shfl_sync(kFull, newcur, s);
+            if (((fa >> s) & 1u) && ncs != INT_MAX && (int64_t)ds[k] >= win) {
+              if ((int64_t)ds[k] >= his)
+                rem |= 1u << s;
+              else
+                mv |= 1u << s;
+            }
+          }
+        }
+        uint32_t todo = few ? 0u : __ballot_sync(kFull, (fml & A) != 0u);
         while (todo) {
           int32_t js[4], vs[4];
           bool hs[4];
@@ -465,29 +577,21 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
           }
         }
         if (mine && rem != fml) S.far[vl] = rem;
-        const bool app = mine && rem != 0u;
-        const uint32_t am = __ballot_sync(kFull, app);
-        if (am) {
-          int32_t base = 0;
-          if (lane == 0) base = atomicAdd(S.cnt + 3 + (p ^ 1), __popc(am));
-          base = __shfl_sync(kFull, base, 0);
-          if (app) {
-            const int32_t pos = base + __popc(am & ((1u << lane) - 1u));
-            if (pos < S.V)
-              S.fl[p ^ 1][pos] = vl;
-            else
-              atomicOr(S.err, DEV_ERR_OVERFLOW);
-          }
-        }
+        if (relist) stl.push(mine && rem != 0u, vl, S.err);
+        bool one = false;
         if (mine && mv) {
           if (atomicMax(S.qstamp + vl, it) < it) {
             S.fr[vl] = mv;
-            bs_enqueue(S, qo, qcnt_out, vl);
+            one = S.off[vl + 1] - S.off[vl] <= S.chunk;
+            if (!one) bs_enqueue(S, qo, qcnt_out, vl);
           } else {
             atomicOr(S.fr + vl, mv);
           }
         }
+        stq.push(one, (int64_t)vl << 32, S.err);
       }
+      stq.flush(S.err);
+      stl.flush(S.err);
       if (blockIdx.x == 0 && threadIdx.x < kLanes) S.cur[(p ^ 1) * kLanes + threadIdx.x] = newcur;
       if (!grid_barrier(S.bar, gridDim.x, S.err, S.timeout_ns)) break;
       ++adv;
