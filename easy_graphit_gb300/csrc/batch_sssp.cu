@@ -41,12 +41,28 @@
 namespace gg {
 
 constexpr int32_t kLanes = kBsLanes;
-constexpr int32_t kPrefetch = 8;  // distance lines in flight per warp
 // Queue entries active for at most S.ep_max sources are relaxed edge-parallel
 // (lanes = edges); busier ones source-parallel (lanes = sources).  S.chunk
 // (edges per queue entry) and S.ep_max come from the graph's batch tuning.
 
 constexpr uint32_t kFull = 0xffffffffu;
+
+// 16-byte asynchronous copy global -> shared (L2 only), and its wait.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(__cvta_generic_to_global(gmem))
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Fire-and-forget global reductions: the relax never uses the old value, and
+// plain atomics on generic pointers compile to value-returning atomics.
+__device__ __forceinline__ void red_min(int32_t *p, int32_t v) {
+  asm volatile("red.relaxed.gpu.global.min.s32 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "r"(v) : "memory");
+}
+__device__ __forceinline__ void red_or(uint32_t *p, uint32_t v) {
+  asm volatile("red.relaxed.gpu.global.or.b32 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "r"(v) : "memory");
+}
 constexpr int32_t kBsScanDiv = 64;  // relaxes over >= V/64 entries mark masks without queueing
 
 // Queues v as ceil(deg/chunk) entries.  The threads of a warp that enqueue
@@ -159,7 +175,7 @@ __device__ __forceinline__ void bs_far_push(const BsState &S, int p, int32_t v) 
 __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64_t n, const int64_t *qi,
                                          const int64_t *hqi, int64_t *qo,
                                          int32_t *qcnt_out, int32_t cut, const int32_t *s_cut, int p,
-                                         int32_t it, int32_t *wctr, int64_t nwarps, bool scan) {
+                                         int32_t it, int32_t *wctr, int64_t nwarps, bool scan, int32_t *dl) {
   const int32_t lane = threadIdx.x & 31;
   for (;;) {
     int32_t e0 = 0, B = 1;
@@ -233,16 +249,16 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64
               const int32_t s = ss[t];
               const int32_t np = du[t] + w;
               if (np < dv[t]) {
-                atomicMin(S.dist + (int64_t)v * kLanes + s, np);
+                red_min(S.dist + (int64_t)v * kLanes + s, np);
                 if (np < s_cut[s]) {
                   if (scan) {
-                    atomicOr(S.nacc + v, 1u << s);
+                    red_or(S.nacc + v, 1u << s);
                   } else if (atomicOr(S.nacc + v, 1u << s) == 0u) {
                     S.qstamp[v] = it;
                     bs_enqueue_first(S, qo, qcnt_out, v);
                   }
                 } else if (scan) {
-                  atomicOr(S.far + v, 1u << s);
+                  red_or(S.far + v, 1u << s);
                 } else if (atomicOr(S.far + v, 1u << s) == 0u) {
                   bs_far_push(S, p, v);
                 }
@@ -252,7 +268,10 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64
         }
       }
     }
-    // (b) busy entries: lane = source, one entry at a time
+    // (b) busy entries: lane = source, one entry at a time.  The distance
+    // lines of 32 edges are gathered into the warp's shared buffer with
+    // cp.async (one round trip per 32 edges, no registers held); lane t then
+    // collects edge t's near / far source masks and updates its vertex.
     uint32_t dense = __ballot_sync(kFull, !sparse && cnt > 0);
     while (dense) {
       const int32_t j = __ffs(dense) - 1;
@@ -271,50 +290,44 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64
           ww = __ldg(S.w + k0 + lane);
         }
         const int32_t cn = min(32, eend - k0);
-        for (int32_t j0 = 0; j0 < cn; j0 += kPrefetch) {
-          // Issue the distance-line loads of kPrefetch edges before using
-          // them.  A stale (larger) value only costs an extra atomicMin.
-          int32_t vs[kPrefetch], ws[kPrefetch], dvs[kPrefetch];
-#pragma unroll
-          for (int32_t t = 0; t < kPrefetch; ++t) {
-            vs[t] = __shfl_sync(kFull, vv, (j0 + t) & 31);
-            ws[t] = __shfl_sync(kFull, ww, (j0 + t) & 31);
-            dvs[t] = (live && j0 + t < cn) ? __ldcg(S.dist + (int64_t)vs[t] * kLanes + lane) : INT_MIN;
-          }
-          // lane t collects edge t's near / far source masks; the vertex
-          // updates of the kPrefetch edges then run on lanes 0..kPrefetch-1
-          int32_t my_v = 0;
-          uint32_t my_nb = 0, my_fb = 0;
-#pragma unroll
-          for (int32_t t = 0; t < kPrefetch; ++t) {
-            if (j0 + t >= cn) break;  // warp-uniform
-            bool near = false, farb = false;
-            if (live) {
-              const int32_t np = du + ws[t];
-              if (np < dvs[t]) {
-                atomicMin(S.dist + (int64_t)vs[t] * kLanes + lane, np);
-                near = np < cut;
-                farb = !near;
-              }
-            }
-            const uint32_t nb = __ballot_sync(kFull, near);
-            const uint32_t fb = __ballot_sync(kFull, farb);
-            if (lane == t) {
-              my_v = vs[t];
-              my_nb = nb;
-              my_fb = fb;
+        // lane l copies sources 4(l%8) .. 4(l%8)+3 of edge q + l/8
+        for (int32_t q = 0; q < cn; q += 4) {
+          const int32_t t = q + (lane >> 3);
+          const int32_t vt = __shfl_sync(kFull, vv, t & 31);
+          if (t < cn) cp_async16(dl + t * kLanes + (lane & 7) * 4, S.dist + (int64_t)vt * kLanes + (lane & 7) * 4);
+        }
+        cp_async_wait_all();
+        __syncwarp();
+        uint32_t my_nb = 0, my_fb = 0;
+        for (int32_t t = 0; t < cn; ++t) {
+          const int32_t vt = __shfl_sync(kFull, vv, t);
+          const int32_t wt = __shfl_sync(kFull, ww, t);
+          bool near = false, farb = false;
+          if (live) {
+            const int32_t np = du + wt;
+            if (np < dl[t * kLanes + lane]) {
+              red_min(S.dist + (int64_t)vt * kLanes + lane, np);
+              near = np < cut;
+              farb = !near;
             }
           }
-          if (scan) {
-            if (my_nb) atomicOr(S.nacc + my_v, my_nb);
-            if (my_fb) atomicOr(S.far + my_v, my_fb);
-          } else {
-            if (my_nb && atomicOr(S.nacc + my_v, my_nb) == 0u) {
-              S.qstamp[my_v] = it;
-              bs_enqueue_first(S, qo, qcnt_out, my_v);
-            }
-            if (my_fb && atomicOr(S.far + my_v, my_fb) == 0u) bs_far_push(S, p, my_v);
+          const uint32_t nb = __ballot_sync(kFull, near);
+          const uint32_t fb = __ballot_sync(kFull, farb);
+          if (lane == t) {
+            my_nb = nb;
+            my_fb = fb;
           }
+        }
+        __syncwarp();  // the buffer is refilled by the next group
+        if (scan) {
+          if (my_nb) red_or(S.nacc + vv, my_nb);
+          if (my_fb) red_or(S.far + vv, my_fb);
+        } else {
+          if (my_nb && atomicOr(S.nacc + vv, my_nb) == 0u) {
+            S.qstamp[vv] = it;
+            bs_enqueue_first(S, qo, qcnt_out, vv);
+          }
+          if (my_fb && atomicOr(S.far + vv, my_fb) == 0u) bs_far_push(S, p, vv);
         }
       }
     }
@@ -324,8 +337,12 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64
 __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
   __shared__ int32_t red[256 / 32][kLanes];
   __shared__ int32_t s_cut[kLanes];
-  __shared__ int64_t s_stq[256 / 32][kStage];  // staged queue entries per warp
-  __shared__ int32_t s_stl[256 / 32][kStage];  // staged far-list entries per warp
+  // per warp: 32 gathered distance lines (relax), or the staged queue and
+  // far-list appends (publish, advance)
+  __shared__ alignas(16) int32_t s_wbuf[256 / 32][32 * kLanes];
+  static_assert(kStage * (sizeof(int64_t) + sizeof(int32_t)) <= sizeof(s_wbuf[0]), "staging fits the warp buffer");
+  int64_t *const s_stq = reinterpret_cast<int64_t *>(s_wbuf[threadIdx.x >> 5]);
+  int32_t *const s_stl = s_wbuf[threadIdx.x >> 5] + 2 * kStage;
   const int32_t lane = threadIdx.x & 31;
   const int32_t wib = threadIdx.x >> 5;
   const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -360,12 +377,12 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
       if (threadIdx.x < kLanes) s_cut[threadIdx.x] = cut;
       __syncthreads();
       bs_relax(S, n, (int64_t)n + nh, S.q[in], S.hq[in], S.q[in ^ 1], qcnt_out, cut, s_cut, p, it, S.wctr + it % 3,
-               nwarps, scan);
+               nwarps, scan, s_wbuf[wib]);
     }
     if (!grid_barrier(S.bar, gridDim.x, S.err, S.timeout_ns)) break;
     // ---- publish near masks of the queued vertices; OR them into the active set
     if (scan) {  // queue every vertex with a near mask, all its chunks
-      WarpStage<int64_t> stq{s_stq[wib], S.q[in ^ 1], qcnt_out, S.qcap, 0};
+      WarpStage<int64_t> stq{s_stq, S.q[in ^ 1], qcnt_out, S.qcap, 0};
       uint32_t act = 0;
       for (int64_t v0 = tid - lane; v0 < S.V; v0 += tstride) {
         const int64_t v = v0 + lane;
@@ -509,8 +526,8 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
       const int32_t newcur = adv_l ? gm : curl;
       const int64_t hi = (int64_t)newcur + S.delta;
       int64_t *qo = S.q[in ^ 1];
-      WarpStage<int64_t> stq{s_stq[wib], qo, qcnt_out, S.qcap, 0};
-      WarpStage<int32_t> stl{s_stl[wib], S.fl[p ^ 1], S.cnt + 3 + (p ^ 1), S.V, 0};
+      WarpStage<int64_t> stq{s_stq, qo, qcnt_out, S.qcap, 0};
+      WarpStage<int32_t> stl{s_stl, S.fl[p ^ 1], S.cnt + 3 + (p ^ 1), S.V, 0};
       for (int64_t e0 = gwarp * FB; e0 < fcount; e0 += nwarps * FB) {
         const int64_t e = e0 + lane;
         const bool mine = lane < FB && e < fcount;
@@ -739,6 +756,8 @@ gg_status bsssp_enqueue(gg_graph *g, cudaStream_t st, const BsState &S, const in
   int per_sm = 0;
   GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bsssp, 256, 0));
   if (per_sm < 1) return set_error(GG_ERR_UNSUPPORTED, "batched SSSP kernel does not fit an SM");
+  if (reinterpret_cast<uintptr_t>(S.dist) % 16 != 0)  // the relax copies distance lines 16 bytes at a time
+    return set_error(GG_ERR_INVALID, "batched SSSP distance buffer is not 16-byte aligned");
   note_launch();
   k_bsssp_init<<<g->sm_count * 8, 256, 0, st>>>(S, dsrc, k);
   note_launch();
