@@ -126,6 +126,7 @@ SIGNATURES: dict[str, tuple] = {
     "gg_bc": (i32, [P, C.POINTER(gg_app_schedule), i32, P, C.POINTER(gg_stats)]),
     "gg_debug_barrier_timeout": (i32, [i32]),
     "gg_kernel_launches": (C.c_uint64, []),
+    "gg_memory_trim": (i32, [C.c_size_t]),
     "gg_bfs_noalloc": (i32, [P, P, i32, i32, i32, P, P]),
     "gg_bfs_batch": (i32, [P, P, i32, P, C.POINTER(gg_stats)]),
     "gg_bc_batch": (i32, [P, P, i32, P, C.POINTER(gg_stats)]),

@@ -173,7 +173,7 @@ gg_status scratch_get_app(gg_graph *g, int slot, size_t bytes, void **p) {
     if (s.p) cudaFreeAsync(s.p, g->stream);
     s.p = nullptr;
     s.bytes = 0;
-    GG_CUDA(cudaMallocAsync(&s.p, bytes, g->stream));
+    GG_CUDA(dev_alloc(&s.p, bytes, g->stream));
     s.bytes = bytes;
   }
   *p = s.p;

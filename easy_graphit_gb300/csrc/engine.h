@@ -114,6 +114,15 @@ struct VData {
 VData to_vdata(const gg_vertex_data *vd);
 
 // ---- graph.cu
+// Stream-ordered device allocation from the library's own memory pool (one
+// per device).  The pool keeps freed memory for reuse instead of handing it
+// back to the driver at every synchronisation, so a graph or batch created
+// after another one was released maps no new pages; gg_memory_trim returns it.
+cudaError_t dev_alloc(void **p, size_t bytes, cudaStream_t st);
+template <typename T>
+inline cudaError_t dev_alloc(T **p, size_t bytes, cudaStream_t st) {
+  return dev_alloc(reinterpret_cast<void **>(p), bytes, st);
+}
 gg_status ensure_transpose(gg_graph *g);
 gg_status ensure_coo(GraphStore &s, cudaStream_t st);
 gg_status ensure_blocked(gg_graph *g, bool reverse, int32_t block_size, const GraphStore **out);

@@ -296,14 +296,14 @@ static gg_status frontier_alloc(gg_frontier *f) {
   f->cap = (int64_t)kFrontierMultiplier * V;
   f->nwords = ceil_div(V, 32);
   f->bytes_padded = f->nwords * 32;  // boolmap padded to whole bitmap words
-  GG_CUDA(cudaMallocAsync(&f->q_in, sizeof(int32_t) * f->cap, st));
-  GG_CUDA(cudaMallocAsync(&f->q_out, sizeof(int32_t) * f->cap, st));
-  GG_CUDA(cudaMallocAsync(&f->cnt, sizeof(int32_t) * 2, st));
-  GG_CUDA(cudaMallocAsync(&f->bm_in, sizeof(uint32_t) * f->nwords, st));
-  GG_CUDA(cudaMallocAsync(&f->bm_out, sizeof(uint32_t) * f->nwords, st));
-  GG_CUDA(cudaMallocAsync(&f->by_in, f->bytes_padded, st));
-  GG_CUDA(cudaMallocAsync(&f->by_out, f->bytes_padded, st));
-  GG_CUDA(cudaMallocAsync(&f->dedup, sizeof(int32_t) * V, st));
+  GG_CUDA(dev_alloc(&f->q_in, sizeof(int32_t) * f->cap, st));
+  GG_CUDA(dev_alloc(&f->q_out, sizeof(int32_t) * f->cap, st));
+  GG_CUDA(dev_alloc(&f->cnt, sizeof(int32_t) * 2, st));
+  GG_CUDA(dev_alloc(&f->bm_in, sizeof(uint32_t) * f->nwords, st));
+  GG_CUDA(dev_alloc(&f->bm_out, sizeof(uint32_t) * f->nwords, st));
+  GG_CUDA(dev_alloc(&f->by_in, f->bytes_padded, st));
+  GG_CUDA(dev_alloc(&f->by_out, f->bytes_padded, st));
+  GG_CUDA(dev_alloc(&f->dedup, sizeof(int32_t) * V, st));
   f->cnt_in = f->cnt;
   f->cnt_out = f->cnt + 1;
   GG_CUDA(cudaMemsetAsync(f->cnt, 0, sizeof(int32_t) * 2, st));
@@ -671,7 +671,7 @@ gg_status gg_frontier_list_create(gg_graph *g, gg_frontier_list **out) {
   GG_CHECK_ARG(g && out, "bad arguments");
   auto l = new gg_frontier_list();
   l->g = g;
-  if (cudaMallocAsync(&l->vertices, sizeof(int32_t) * (size_t)g->csr.V, g->stream) != cudaSuccess) {
+  if (dev_alloc(&l->vertices, sizeof(int32_t) * (size_t)g->csr.V, g->stream) != cudaSuccess) {
     delete l;
     return set_error(GG_ERR_OOM, "frontier list allocation failed");
   }

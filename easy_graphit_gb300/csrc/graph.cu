@@ -7,6 +7,7 @@
 //    that also frees the source arrays) is a GPU bucketing into a separate copy.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 
 #include "engine.h"
 #include "scan.cuh"
@@ -194,9 +195,40 @@ __global__ void k_bucket_scatter(const int32_t *__restrict__ src, const int32_t 
 
 static int stream_grid(gg_graph *g) { return g->sm_count * 8; }
 
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_pool_mu;
+cudaMemPool_t g_pool[kMaxDevices] = {};
+}  // namespace
+
+cudaError_t dev_alloc(void **p, size_t bytes, cudaStream_t st) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaMallocAsync(p, bytes, st);
+  cudaMemPool_t pool = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_pool[dev]) {
+      cudaMemPoolProps props{};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.handleTypes = cudaMemHandleTypeNone;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      e = cudaMemPoolCreate(&g_pool[dev], &props);
+      if (e != cudaSuccess) return e;
+      uint64_t keep = UINT64_MAX;
+      e = cudaMemPoolSetAttribute(g_pool[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+      if (e != cudaSuccess) return e;
+    }
+    pool = g_pool[dev];
+  }
+  return cudaMallocFromPoolAsync(p, bytes, pool, st);
+}
+
 gg_status ensure_coo(GraphStore &s, cudaStream_t st) {
   if (s.src || s.E == 0) return GG_OK;
-  GG_CUDA(cudaMallocAsync(&s.src, sizeof(int32_t) * (size_t)s.E, st));
+  GG_CUDA(dev_alloc(&s.src, sizeof(int32_t) * (size_t)s.E, st));
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -221,12 +253,12 @@ gg_status ensure_transpose(gg_graph *g) {
   t->E = f.E;
   GG_TRY(ensure_coo(g->csr, st));
   int32_t *cnt = nullptr, *partial = nullptr;
-  GG_CUDA(cudaMallocAsync(&t->off, sizeof(int32_t) * (f.V + 1), st));
-  GG_CUDA(cudaMallocAsync(&t->dst, sizeof(int32_t) * std::max(f.E, 1), st));
-  GG_CUDA(cudaMallocAsync(&t->w, sizeof(int32_t) * std::max(f.E, 1), st));
-  GG_CUDA(cudaMallocAsync(&t->src, sizeof(int32_t) * std::max(f.E, 1), st));
-  GG_CUDA(cudaMallocAsync(&cnt, sizeof(int32_t) * (f.V + 1), st));
-  GG_CUDA(cudaMallocAsync(&partial, sizeof(int32_t) * scan_scratch_ints(f.V), st));
+  GG_CUDA(dev_alloc(&t->off, sizeof(int32_t) * (f.V + 1), st));
+  GG_CUDA(dev_alloc(&t->dst, sizeof(int32_t) * std::max(f.E, 1), st));
+  GG_CUDA(dev_alloc(&t->w, sizeof(int32_t) * std::max(f.E, 1), st));
+  GG_CUDA(dev_alloc(&t->src, sizeof(int32_t) * std::max(f.E, 1), st));
+  GG_CUDA(dev_alloc(&cnt, sizeof(int32_t) * (f.V + 1), st));
+  GG_CUDA(dev_alloc(&partial, sizeof(int32_t) * scan_scratch_ints(f.V), st));
   GG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (f.V + 1), st));
   const int grid = stream_grid(g);
   { gg::note_launch(); k_count_dst<<<grid, 256, 0, st>>>(f.dst, f.E, cnt); }
@@ -256,10 +288,10 @@ gg_status ensure_transpose(gg_graph *g) {
     const int32_t nl = (int32_t)longs.size();
     int32_t *ids = nullptr, *tk = nullptr, *tw = nullptr;
     int64_t *dpoff = nullptr;
-    GG_CUDA(cudaMallocAsync(&ids, sizeof(int32_t) * nl, st));
-    GG_CUDA(cudaMallocAsync(&dpoff, sizeof(int64_t) * (nl + 1), st));
-    GG_CUDA(cudaMallocAsync(&tk, sizeof(int32_t) * poff[nl], st));
-    GG_CUDA(cudaMallocAsync(&tw, sizeof(int32_t) * poff[nl], st));
+    GG_CUDA(dev_alloc(&ids, sizeof(int32_t) * nl, st));
+    GG_CUDA(dev_alloc(&dpoff, sizeof(int64_t) * (nl + 1), st));
+    GG_CUDA(dev_alloc(&tk, sizeof(int32_t) * poff[nl], st));
+    GG_CUDA(dev_alloc(&tw, sizeof(int32_t) * poff[nl], st));
     GG_CUDA(cudaMemcpyAsync(ids, longs.data(), sizeof(int32_t) * nl, cudaMemcpyHostToDevice, st));
     GG_CUDA(cudaMemcpyAsync(dpoff, poff.data(), sizeof(int64_t) * (nl + 1), cudaMemcpyHostToDevice, st));
     dim3 grd((unsigned)std::min<int64_t>(64, (maxp2 + 255) / 256), (unsigned)std::min(nl, 1024));
@@ -298,12 +330,12 @@ gg_status ensure_blocked(gg_graph *g, bool reverse, int32_t block_size, const Gr
   b.nbuckets = (base.V + block_size - 1) / block_size;
   int32_t *cnt = nullptr, *partial = nullptr;
   const size_t E1 = std::max(base.E, 1);
-  GG_CUDA(cudaMallocAsync(&b.src, sizeof(int32_t) * E1, st));
-  GG_CUDA(cudaMallocAsync(&b.dst, sizeof(int32_t) * E1, st));
-  GG_CUDA(cudaMallocAsync(&b.w, sizeof(int32_t) * E1, st));
-  GG_CUDA(cudaMallocAsync(&b.bucket, sizeof(int32_t) * (b.nbuckets + 1), st));
-  GG_CUDA(cudaMallocAsync(&cnt, sizeof(int32_t) * (b.nbuckets + 1), st));
-  GG_CUDA(cudaMallocAsync(&partial, sizeof(int32_t) * scan_scratch_ints(b.nbuckets), st));
+  GG_CUDA(dev_alloc(&b.src, sizeof(int32_t) * E1, st));
+  GG_CUDA(dev_alloc(&b.dst, sizeof(int32_t) * E1, st));
+  GG_CUDA(dev_alloc(&b.w, sizeof(int32_t) * E1, st));
+  GG_CUDA(dev_alloc(&b.bucket, sizeof(int32_t) * (b.nbuckets + 1), st));
+  GG_CUDA(dev_alloc(&cnt, sizeof(int32_t) * (b.nbuckets + 1), st));
+  GG_CUDA(dev_alloc(&partial, sizeof(int32_t) * scan_scratch_ints(b.nbuckets), st));
   GG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (b.nbuckets + 1), st));
   const int grid = stream_grid(g);
   { gg::note_launch(); k_bucket_count<<<grid, 256, 0, st>>>(base.dst, base.E, block_size, cnt); }
@@ -336,7 +368,7 @@ gg_status scratch_get(gg_graph *g, int slot, size_t bytes, void **p) {
     if (s.p) cudaFreeAsync(s.p, g->stream);
     s.p = nullptr;
     s.bytes = 0;
-    GG_CUDA(cudaMallocAsync(&s.p, bytes, g->stream));
+    GG_CUDA(dev_alloc(&s.p, bytes, g->stream));
     s.bytes = bytes;
   }
   *p = s.p;
@@ -374,9 +406,9 @@ gg_status gg_graph_create(const int32_t *offsets, const int32_t *dst, const int3
   s.V = V;
   s.E = (int32_t)E;
   const size_t E1 = std::max<int64_t>(E, 1);
-  GG_CUDA(cudaMallocAsync(&s.off, sizeof(int32_t) * (V + 1), st));
-  GG_CUDA(cudaMallocAsync(&s.dst, sizeof(int32_t) * E1, st));
-  GG_CUDA(cudaMallocAsync(&s.w, sizeof(int32_t) * E1, st));
+  GG_CUDA(dev_alloc(&s.off, sizeof(int32_t) * (V + 1), st));
+  GG_CUDA(dev_alloc(&s.dst, sizeof(int32_t) * E1, st));
+  GG_CUDA(dev_alloc(&s.w, sizeof(int32_t) * E1, st));
   GG_CUDA(cudaMemcpyAsync(s.off, offsets, sizeof(int32_t) * (V + 1), cudaMemcpyDefault, st));
   if (E) {
     GG_CUDA(cudaMemcpyAsync(s.dst, dst, sizeof(int32_t) * E, cudaMemcpyDefault, st));
@@ -388,9 +420,9 @@ gg_status gg_graph_create(const int32_t *offsets, const int32_t *dst, const int3
       GG_CUDA(cudaStreamSynchronize(st));
     }
   }
-  GG_CUDA(cudaMallocAsync(&g->d_err, sizeof(int32_t), st));
-  GG_CUDA(cudaMallocAsync(&g->d_bar, sizeof(uint32_t) * 2, st));
-  GG_CUDA(cudaMallocAsync(&g->d_misc, sizeof(int32_t) * 64, st));
+  GG_CUDA(dev_alloc(&g->d_err, sizeof(int32_t), st));
+  GG_CUDA(dev_alloc(&g->d_bar, sizeof(uint32_t) * 2, st));
+  GG_CUDA(dev_alloc(&g->d_misc, sizeof(int32_t) * 64, st));
   GG_CUDA(cudaMemsetAsync(g->d_err, 0, sizeof(int32_t), st));
   GG_CUDA(cudaMemsetAsync(g->d_bar, 0, sizeof(uint32_t) * 2, st));
   GG_CUDA(cudaMemsetAsync(g->d_misc, 0, sizeof(int32_t) * 64, st));
@@ -477,3 +509,12 @@ gg_status gg_graph_device_arrays(const gg_graph *g, const int32_t **off, const i
 }
 
 }  // extern "C"
+
+// Hands the library pools' unused memory back to the driver, keeping at most
+// keep_bytes reserved per device.
+extern "C" gg_status gg_memory_trim(size_t keep_bytes) {
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  for (int d = 0; d < kMaxDevices; ++d)
+    if (g_pool[d]) GG_CUDA(cudaMemPoolTrimTo(g_pool[d], keep_bytes));
+  return GG_OK;
+}

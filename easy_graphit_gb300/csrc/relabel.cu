@@ -117,16 +117,16 @@ gg_status ensure_relabel(gg_graph *g) {
   r->g.E = f.E;
   const int32_t nb = std::max(1, ceil_div(V, kRlTile));
   int32_t *indeg = nullptr, *hist = nullptr, *base = nullptr, *partial = nullptr;
-  GG_CUDA(cudaMallocAsync(&r->perm, sizeof(int32_t) * std::max(V, 1), st));
-  GG_CUDA(cudaMallocAsync(&r->inv, sizeof(int32_t) * std::max(V, 1), st));
-  GG_CUDA(cudaMallocAsync(&r->g.off, sizeof(int32_t) * (V + 1), st));
-  GG_CUDA(cudaMallocAsync(&r->g.dst, sizeof(int32_t) * std::max(f.E, 1), st));
-  GG_CUDA(cudaMallocAsync(&r->g.w, sizeof(int32_t) * std::max(f.E, 1), st));
-  GG_CUDA(cudaMallocAsync(&indeg, sizeof(int32_t) * std::max(V, 1), st));
-  GG_CUDA(cudaMallocAsync(&hist, sizeof(int32_t) * kRlClasses * nb, st));
-  GG_CUDA(cudaMallocAsync(&base, sizeof(int32_t) * (kRlClasses * nb + 1), st));
+  GG_CUDA(dev_alloc(&r->perm, sizeof(int32_t) * std::max(V, 1), st));
+  GG_CUDA(dev_alloc(&r->inv, sizeof(int32_t) * std::max(V, 1), st));
+  GG_CUDA(dev_alloc(&r->g.off, sizeof(int32_t) * (V + 1), st));
+  GG_CUDA(dev_alloc(&r->g.dst, sizeof(int32_t) * std::max(f.E, 1), st));
+  GG_CUDA(dev_alloc(&r->g.w, sizeof(int32_t) * std::max(f.E, 1), st));
+  GG_CUDA(dev_alloc(&indeg, sizeof(int32_t) * std::max(V, 1), st));
+  GG_CUDA(dev_alloc(&hist, sizeof(int32_t) * kRlClasses * nb, st));
+  GG_CUDA(dev_alloc(&base, sizeof(int32_t) * (kRlClasses * nb + 1), st));
   const size_t scan_n = std::max<size_t>(V, (size_t)kRlClasses * nb);
-  GG_CUDA(cudaMallocAsync(&partial, sizeof(int32_t) * scan_scratch_ints((int64_t)scan_n), st));
+  GG_CUDA(dev_alloc(&partial, sizeof(int32_t) * scan_scratch_ints((int64_t)scan_n), st));
   const int grid = g->sm_count * 8;
   if (g->symmetric) {
     note_launch();
@@ -160,10 +160,10 @@ gg_status ensure_relabel_csc(gg_graph *g) {
   Relabeled &r = *g->rel;
   const int32_t V = t.V;
   int32_t *partial = nullptr;
-  GG_CUDA(cudaMallocAsync(&r.csc.off, sizeof(int32_t) * (V + 1), st));
-  GG_CUDA(cudaMallocAsync(&r.csc.dst, sizeof(int32_t) * std::max(t.E, 1), st));
-  GG_CUDA(cudaMallocAsync(&r.csc.w, sizeof(int32_t) * std::max(t.E, 1), st));
-  GG_CUDA(cudaMallocAsync(&partial, sizeof(int32_t) * scan_scratch_ints(V), st));
+  GG_CUDA(dev_alloc(&r.csc.off, sizeof(int32_t) * (V + 1), st));
+  GG_CUDA(dev_alloc(&r.csc.dst, sizeof(int32_t) * std::max(t.E, 1), st));
+  GG_CUDA(dev_alloc(&r.csc.w, sizeof(int32_t) * std::max(t.E, 1), st));
+  GG_CUDA(dev_alloc(&partial, sizeof(int32_t) * scan_scratch_ints(V), st));
   r.csc.V = V;
   r.csc.E = t.E;
   GG_CUDA(exclusive_scan(RlDegIn{t.off, r.inv}, V, r.csc.off, partial, st));

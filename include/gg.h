@@ -307,6 +307,12 @@ typedef struct gg_stats {
 /* Number of kernels libgg.so has launched in this process. */
 uint64_t gg_kernel_launches(void);
 
+/* Device memory released by graphs, frontiers and batches stays in the
+ * library's stream-ordered pool for reuse (a new graph maps no new pages).
+ * gg_memory_trim hands the unused part back to the driver, keeping at most
+ * keep_bytes reserved per device. */
+gg_status gg_memory_trim(size_t keep_bytes);
+
 /* BFS from src: depth_out[v] = hop distance (-1 unreached); parent_out (may be
  * NULL) = the parent array of bfs.cpp (parent[src] = src). */
 gg_status gg_bfs(gg_graph *g, const gg_app_schedule *s, int32_t src,
