@@ -306,3 +306,30 @@ def test_cc_fused_union_find_matches_the_rounds(kind):
     np.testing.assert_array_equal(fused, oracle.cc(off, dst))
     np.testing.assert_array_equal(fused, rounds)
     assert st["fused"] == 1
+
+
+@pytest.mark.parametrize("symmetrize", [False, True])
+def test_cc_fused_when_the_giant_tree_joins_a_smaller_root_late(symmetrize):
+    """The union-find pass skips the vertices of the most frequent sampled root
+    c after two sampling rounds.  Here component B = {0..99} (a path) reaches the
+    giant component A = {1000..4999} only through edges 50 -> 3000 and 60 -> 4000
+    that come after the first two entries of their out-lists, so on the directed
+    graph they are never sampled and c's tree must be hooked under B's root 0
+    during the finishing pass.  Vertices 100..999 are isolated, 5000..5009 form a
+    ring of their own."""
+    rng = np.random.default_rng(5)
+    u = [np.arange(1000, 4999), rng.integers(1000, 5000, 20000)]
+    v = [np.arange(1001, 5000), rng.integers(1000, 5000, 20000)]
+    u += [np.arange(0, 99), np.array([50, 50, 50, 60, 60, 60])]
+    v += [np.arange(1, 100), np.array([0, 1, 3000, 2, 3, 4000])]
+    u += [np.arange(5000, 5010)]
+    v += [np.array([5001, 5002, 5003, 5004, 5005, 5006, 5007, 5008, 5009, 5000])]
+    hg = HostGraph.from_edges(5010, np.concatenate(u), np.concatenate(v), symmetrize=symmetrize)
+    g = GraphT(hg, symmetric=symmetrize)
+    off, dst = np.array(hg.offsets), np.array(hg.dst)
+    sch, _ = default_schedule("cc")
+    fused, st = cc(g, sch, True)
+    ref = oracle.cc(off, dst)
+    np.testing.assert_array_equal(fused, ref)
+    assert fused[3000] == 0 and fused[4999] == 0 and fused[500] == 500 and fused[5005] == 5000
+    g.close()
