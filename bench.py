@@ -56,6 +56,8 @@ def parse():
                         "(built-in) or 'B,C,E' (CTAs per SM, chunk, edge-parallel threshold)")
     p.add_argument("--no-apps", action="store_true",
                    help="omit the per-app comparison lines (BFS, BC, PageRank)")
+    p.add_argument("--no-sweep", action="store_true",
+                   help="omit the delta sweep on this graph and the 4096 x 4096 grid")
     return p.parse_args()
 
 
@@ -348,6 +350,7 @@ def run_gb300(args):
     e2e_val, e2e_ms = aggregate_teps(total_edges, e2e_ms, device=dev)
 
     apps = None if args.no_apps else per_app(g, hg, off, dst, dev, stream, peaks()[0])
+    sweep = None if args.no_sweep else delta_sweep(g, h_src, dist_dev, total_edges, dev)
 
     if rank != 0:
         if world > 1:
@@ -394,10 +397,74 @@ def run_gb300(args):
         "clocks": clk.summary(),
         "gpu_launches": launches,
         "apps": apps,
+        "sssp_sweep": sweep,
     }
     print(json.dumps(out))
     if world > 1:
         dist.destroy_process_group()
+
+
+def delta_sweep(g, h_src, dist_dev, total_edges, dev):
+    """Batched SSSP (32 sources, one launch) over the delta sweep {1, 8, 32, 128}
+    on this graph, and on the 4096 x 4096 4-neighbour grid (weights U[1,1000],
+    high diameter) at delta 128 and 32 -- there delta 8 and 1 take 3 x 10^5 and
+    more buckets (17 s and more per launch).  Loop time by CUDA events; the
+    GAPBS ordered-processing port on the host cores runs one grid source at the
+    same deltas beside it.  All deltas give the same distances (checked)."""
+    import ctypes as C
+
+    import torch
+
+    import oracle
+    from easy_graphit_gb300 import GraphT, HostGraph, _lib as L
+    st = L.gg_stats()
+    nsrc = len(h_src)
+
+    def launch(gr, srcs, delta, out):
+        L.call("gg_sssp_batch", gr.handle, C.c_void_p(srcs.ctypes.data), len(srcs), delta,
+               C.c_void_p(out.data_ptr()), C.byref(st))
+        return st.loop_ms
+
+    ref = dist_dev.clone()
+    rmat = {}
+    for d in DELTAS:
+        launch(g, h_src, d, dist_dev)
+        ms = min(launch(g, h_src, d, dist_dev) for _ in range(2))
+        assert torch.equal(dist_dev, ref), f"delta {d} changed the distances"
+        rmat[str(d)] = {"loop_ms": ms, "gteps": total_edges / ms / 1e6}
+    del ref
+    hg = HostGraph.grid(4096, 4096)
+    gg = GraphT(hg, symmetric=True)
+    srcs = np.ascontiguousarray(hg.pick_sources(nsrc), dtype=np.int32)
+    out = torch.empty((nsrc, hg.num_vertices), dtype=torch.int32, device=dev)
+    deg = torch.from_numpy(np.diff(np.array(hg.offsets)).astype(np.int64)).to(dev)
+    grid = {}
+    first = None
+    for d in (128, 128, 32):
+        ms = launch(gg, srcs, d, out)
+        reached = out != INT_MAX
+        e_r = float((reached.to(torch.int64) * deg).sum())
+        if first is None:
+            first = out.clone()
+            continue
+        assert torch.equal(out, first), f"delta {d} changed the grid distances"
+        grid[str(d)] = {"loop_ms": ms, "gteps": e_r / ms / 1e6,
+                        "bucket_advances": int(st.bucket_advances), "iterations": int(st.iterations)}
+    off, dstg, w = np.array(hg.offsets), np.array(hg.dst), np.array(hg.weights)
+    cpu = {}
+    for d in (128, 32):
+        t0 = time.perf_counter()
+        dd = oracle.sssp_ordered(off, dstg, w, int(srcs[0]), d, os.cpu_count() or 1)
+        t = time.perf_counter() - t0
+        cpu[str(d)] = {"seconds_one_source": t, "gteps": reached_stats(off, dd)[1] / t / 1e9}
+    gg.close()
+    return {"rmat22_batched": rmat,
+            "grid4096_batched": grid,
+            "grid4096_cpu_port": cpu,
+            "grid": "4096 x 4096 4-neighbour, both directions, weights U[1,1000] (V 16,777,216, E 67,092,480)",
+            "note": "one timed launch per delta on the grid (after an untimed one at delta 128); "
+                    "built-in launch shape; CPU: GAPBS OrderedProcessingOperatorNoMerge port, one source, "
+                    "all host threads"}
 
 
 def per_app(g, hg, off, dst, dev, stream, peak):
