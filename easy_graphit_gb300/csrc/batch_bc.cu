@@ -389,7 +389,9 @@ gg_status bcb_buffers(gg_graph *g, bool owned, BcBuffers *b) {
     return set_error(GG_ERR_UNSUPPORTED, "batched BC holds 64 level-list entries per vertex in int32: "
                                          "V = %d is too large (use gg_bc)", V);
   GG_TRY(ensure_transpose(g));
-  if (g->symmetric) GG_TRY(ensure_relabel(g));  // one degree-ordered copy serves both directions
+  // walk the degree-ordered copy: the rows of the most-gathered vertices share L2
+  GG_TRY(ensure_relabel(g));
+  if (!g->symmetric) GG_TRY(ensure_relabel_csc(g));  // its in-lists (a symmetric copy serves both)
   b->owned = owned;
   const size_t sz[6] = {sizeof(uint64_t) * 8 * (size_t)V, sizeof(int32_t) * bc_int_words(V),
                         sizeof(int64_t) * (size_t)bc_wcap(g), sizeof(uint16_t) * kBcWidth * (size_t)V,
@@ -411,8 +413,8 @@ gg_status bcb_buffers(gg_graph *g, bool owned, BcBuffers *b) {
 
 static BcState bcb_state(gg_graph *g, const BcBuffers &b, int32_t k) {
   const int32_t V = g->csr.V;
-  const bool rel = g->symmetric && g->rel;
-  const GraphStore &t = rel ? g->rel->g : (g->csc ? *g->csc : g->csr);
+  const bool rel = g->rel && (g->symmetric || g->rel->csc.off);
+  const GraphStore &t = rel ? (g->symmetric ? g->rel->g : g->rel->csc) : (g->csc ? *g->csc : g->csr);
   BcState S{};
   S.perm = rel ? g->rel->perm : nullptr;
   S.seen = b.masks;
@@ -468,7 +470,7 @@ gg_status bcb_enqueue(gg_graph *g, cudaStream_t st, const BcBuffers &b, int32_t 
   note_launch();
   k_bcb_seed<<<1, 32, 0, st>>>(S, dsrc);
   GG_CUDA(cudaMemsetAsync(S.bar, 0, sizeof(uint32_t) * 2, st));
-  DGraph dg = (g->symmetric && g->rel) ? g->rel->g.view() : g->csr.view();
+  DGraph dg = (S0.perm != nullptr) ? g->rel->g.view() : g->csr.view();
   dg.nbuckets = 0;
   void *args[] = {&dg, &S};
   if (timed) GG_CUDA(cudaEventRecord(g->ev2, st));
