@@ -12,10 +12,17 @@
 // with cutoff cur[s]+delta; an improvement below the cutoff sets s in v's near
 // mask and queues v, one at or above it sets s in v's far mask and puts v on the
 // far list.  When source s has no near work left, it advances: cur[s] becomes
-// the smallest far priority >= cur[s]+delta, and far entries inside
-// [cur[s], cur[s]+delta) move to the near frontier.  Every vertex whose priority
-// is at or above the window was last improved at or above a cutoff, so the far
-// list holds exactly the candidates the reference finds by scanning all V.
+// the smallest far priority recorded for s since its last advance, and far
+// entries inside [cur[s], cur[s]+delta) move to the near frontier.  Every vertex
+// whose priority is at or above the window was last improved at or above a
+// cutoff, so the far list holds exactly the candidates the reference finds by
+// scanning all V.  The recorded minimum (relaxes fold their far values into a
+// per-CTA minimum, the advance folds in what it keeps) is never above the
+// smallest pending far priority and never below the old window; it equals the
+// reference's next window (gpu_priority_queue.h: min P[v] >= cur+delta) unless
+// that vertex has since been settled through a lighter path, and then the
+// window only starts lower -- at worst it is empty and the next advance starts
+// from exact minima.  Distances are the same either way.
 //
 // A relaxation registers (near or far) when its value is below the distance
 // read before its atomicMin, which is issued without waiting for the old value:
@@ -31,7 +38,7 @@
 // with thousands of small iterations never pay a V-sized scan per iteration.
 //
 // Iteration: relax | barrier | publish near masks, collect the active sources |
-// barrier | [advance pass 1 (minima) | barrier | pass 2 (move/keep) | barrier].
+// barrier | [advance: move / keep far entries | barrier].
 #include <cooperative_groups/scan.h>
 
 #include <algorithm>
@@ -175,7 +182,8 @@ __device__ __forceinline__ void bs_far_push(const BsState &S, int p, int32_t v) 
 __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64_t n, const int64_t *qi,
                                          const int64_t *hqi, int64_t *qo,
                                          int32_t *qcnt_out, int32_t cut, const int32_t *s_cut, int p,
-                                         int32_t it, int32_t *wctr, int64_t nwarps, bool scan, int32_t *dl) {
+                                         int32_t it, int32_t *wctr, int64_t nwarps, bool scan, int32_t *dl,
+                                         int32_t *s_fmin) {
   const int32_t lane = threadIdx.x & 31;
   for (;;) {
     int32_t e0 = 0, B = 1;
@@ -257,10 +265,13 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64
                     S.qstamp[v] = it;
                     bs_enqueue_first(S, qo, qcnt_out, v);
                   }
-                } else if (scan) {
-                  red_or(S.far + v, 1u << s);
-                } else if (atomicOr(S.far + v, 1u << s) == 0u) {
-                  bs_far_push(S, p, v);
+                } else {
+                  if (np < *(volatile int32_t *)(s_fmin + s)) atomicMin(s_fmin + s, np);
+                  if (scan) {
+                    red_or(S.far + v, 1u << s);
+                  } else if (atomicOr(S.far + v, 1u << s) == 0u) {
+                    bs_far_push(S, p, v);
+                  }
                 }
               }
             }
@@ -273,6 +284,7 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64
     // cp.async (one round trip per 32 edges, no registers held); lane t then
     // collects edge t's near / far source masks and updates its vertex.
     uint32_t dense = __ballot_sync(kFull, !sparse && cnt > 0);
+    int32_t fmin = INT_MAX;  // lane = source: smallest far value this warp produced
     while (dense) {
       const int32_t j = __ffs(dense) - 1;
       dense &= dense - 1;
@@ -309,6 +321,7 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64
               red_min(S.dist + (int64_t)vt * kLanes + lane, np);
               near = np < cut;
               farb = !near;
+              if (farb && np < fmin) fmin = np;
             }
           }
           const uint32_t nb = __ballot_sync(kFull, near);
@@ -331,12 +344,13 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64
         }
       }
     }
+    if (fmin != INT_MAX && fmin < *(volatile int32_t *)(s_fmin + lane)) atomicMin(s_fmin + lane, fmin);
   }
 }
 
 __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
-  __shared__ int32_t red[256 / 32][kLanes];
   __shared__ int32_t s_cut[kLanes];
+  __shared__ int32_t s_fmin[kLanes];  // this CTA's smallest far value per source
   // per warp: 32 gathered distance lines (relax), or the staged queue and
   // far-list appends (publish, advance)
   __shared__ alignas(16) int32_t s_wbuf[256 / 32][32 * kLanes];
@@ -374,10 +388,20 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
       const int32_t curl = __ldcg(S.cur + p * kLanes + lane);
       const int64_t cl = (int64_t)curl + S.delta;
       const int32_t cut = cl > INT_MAX ? INT_MAX : (int32_t)cl;
-      if (threadIdx.x < kLanes) s_cut[threadIdx.x] = cut;
+      if (threadIdx.x < kLanes) {
+        s_cut[threadIdx.x] = cut;
+        s_fmin[threadIdx.x] = INT_MAX;
+      }
+      // the minima the next advance accumulates and the far list it rebuilds
+      // were last read by the previous advance
+      if (blockIdx.x == 0 && threadIdx.x < kLanes) S.gmin[(p ^ 1) * kLanes + threadIdx.x] = INT_MAX;
+      if (blockIdx.x == 0 && threadIdx.x == 0) S.cnt[3 + (p ^ 1)] = 0;
       __syncthreads();
       bs_relax(S, n, (int64_t)n + nh, S.q[in], S.hq[in], S.q[in ^ 1], qcnt_out, cut, s_cut, p, it, S.wctr + it % 3,
-               nwarps, scan, s_wbuf[wib]);
+               nwarps, scan, s_wbuf[wib], s_fmin);
+      __syncthreads();
+      if (threadIdx.x < kLanes && s_fmin[threadIdx.x] != INT_MAX)
+        atomicMin(S.gmin + p * kLanes + threadIdx.x, s_fmin[threadIdx.x]);
     }
     if (!grid_barrier(S.bar, gridDim.x, S.err, S.timeout_ns)) break;
     // ---- publish near masks of the queued vertices; OR them into the active set
@@ -440,6 +464,7 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
     }
     const uint32_t active = (uint32_t)*(volatile int32_t *)(S.cnt + 5 + it % 3);
     const uint32_t A = unfinished & ~active;
+    bool pending = false;  // a source is left whose new window came out empty
     if (A) {
       // after a scanning relax the far list misses vertices: walk all V instead
       const bool fscan = fdirty;
@@ -453,74 +478,16 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
       const int32_t curl = __ldcg(S.cur + p * kLanes + lane);
       const int64_t window = (int64_t)curl + S.delta;
       const bool adv_l = (A >> lane) & 1u;
-      if (blockIdx.x == 0 && threadIdx.x < kLanes) {
-        S.gmin[(p ^ 1) * kLanes + threadIdx.x] = INT_MAX;
-        if (threadIdx.x == 0) S.cnt[3 + (p ^ 1)] = 0;
-      }
-      // pass 1: per-source minimum far priority at or above the window.
-      // Lane l loads far entry l of the warp's 32; the distance lines of the
-      // entries with advancing sources are then loaded 4 at a time (or, for
-      // at most kAdvFew advancing sources, lane = entry).
+      // The new window of an advancing source starts at the smallest far value
+      // recorded for it since its last advance (relaxes and the kept entries of
+      // that advance add to S.gmin[p]).  That is at most every far entry still
+      // pending, so nothing is skipped; a value that has since dropped into an
+      // earlier window makes at worst one empty bucket.
       const int32_t nA = __popc(A);
       const bool few = nA <= kAdvFew;
-      int32_t mn = INT_MAX;
       const int32_t FB = bs_batch(fcount, nwarps);
-      for (int64_t e0 = gwarp * FB; e0 < fcount; e0 += nwarps * FB) {
-        const int64_t e = e0 + lane;
-        int32_t vl = 0;
-        uint32_t fml = 0;
-        if (lane < FB && e < fcount) {
-          vl = fscan ? (int32_t)e : __ldcg(fla + e);
-          fml = __ldcg(S.far + vl) & A;
-        }
-        if (few) {
-          int32_t ds[kAdvFew];
-          bs_far_loads(S, vl, fml, A, nA, ds);
-          uint32_t aa = A;
-#pragma unroll
-          for (int32_t k = 0; k < kAdvFew; ++k) {
-            if (k >= nA) break;  // warp-uniform
-            const int32_t s = __ffs(aa) - 1;
-            aa &= aa - 1;
-            const int64_t win = __shfl_sync(kFull, window, s);
-            const int32_t m = __reduce_min_sync(kFull, (int64_t)ds[k] >= win ? ds[k] : INT_MAX);
-            if (lane == s && m < mn) mn = m;
-          }
-          continue;
-        }
-        uint32_t want = __ballot_sync(kFull, fml != 0u);
-        while (want) {
-          int32_t vs[4];
-          bool hs[4];
-#pragma unroll
-          for (int t = 0; t < 4; ++t) {
-            int32_t j = 0;
-            if (want) {
-              j = __ffs(want) - 1;
-              want &= want - 1;
-              hs[t] = (__shfl_sync(kFull, fml, j) >> lane) & 1u;
-            } else {
-              __shfl_sync(kFull, fml, 0);
-              hs[t] = false;
-            }
-            vs[t] = __shfl_sync(kFull, vl, j);
-          }
-          int32_t ds[4];
-#pragma unroll
-          for (int t = 0; t < 4; ++t) ds[t] = hs[t] ? __ldcg(S.dist + (int64_t)vs[t] * kLanes + lane) : INT_MAX;
-#pragma unroll
-          for (int t = 0; t < 4; ++t)
-            if (hs[t] && (int64_t)ds[t] >= window && ds[t] < mn) mn = ds[t];
-        }
-      }
-      red[wib][lane] = mn;
+      if (threadIdx.x < kLanes) s_fmin[threadIdx.x] = INT_MAX;
       __syncthreads();
-      if (threadIdx.x < kLanes) {
-        int32_t mm = INT_MAX;
-        for (int32_t k = 0; k < (int32_t)(blockDim.x >> 5); ++k) mm = min(mm, red[k][threadIdx.x]);
-        if (mm != INT_MAX) atomicMin(S.gmin + p * kLanes + threadIdx.x, mm);
-      }
-      if (!grid_barrier(S.bar, gridDim.x, S.err, S.timeout_ns)) break;
       // pass 2: move [cur', cur'+delta) to the near frontier, keep the rest
       const int32_t gm = __ldcg(S.gmin + p * kLanes + lane);
       const int32_t newcur = adv_l ? gm : curl;
@@ -528,6 +495,7 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
       int64_t *qo = S.q[in ^ 1];
       WarpStage<int64_t> stq{s_stq, qo, qcnt_out, S.qcap, 0};
       WarpStage<int32_t> stl{s_stl, S.fl[p ^ 1], S.cnt + 3 + (p ^ 1), S.V, 0};
+      int32_t kmin = INT_MAX;  // lane = source: smallest value it keeps far
       for (int64_t e0 = gwarp * FB; e0 < fcount; e0 += nwarps * FB) {
         const int64_t e = e0 + lane;
         const bool mine = lane < FB && e < fcount;
@@ -552,12 +520,17 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
             const int64_t win = __shfl_sync(kFull, window, s);
             const int64_t his = __shfl_sync(kFull, hi, s);
             const int32_t ncs = __shfl_sync(kFull, newcur, s);
+            int32_t kept = INT_MAX;
             if (((fa >> s) & 1u) && ncs != INT_MAX && (int64_t)ds[k] >= win) {
-              if ((int64_t)ds[k] >= his)
+              if ((int64_t)ds[k] >= his) {
                 rem |= 1u << s;
-              else
+                kept = ds[k];
+              } else {
                 mv |= 1u << s;
+              }
             }
+            const int32_t km = __reduce_min_sync(kFull, kept);
+            if (lane == 0 && km != INT_MAX && km < *(volatile int32_t *)(s_fmin + s)) atomicMin(s_fmin + s, km);
           }
         }
         uint32_t todo = few ? 0u : __ballot_sync(kFull, (fml & A) != 0u);
@@ -585,6 +558,7 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
             const bool in_win = hs[t] && (int64_t)ds[t] >= window;
             const bool keep = in_win && (int64_t)ds[t] >= hi;
             const bool move = in_win && (int64_t)ds[t] < hi;
+            if (keep && ds[t] < kmin) kmin = ds[t];
             const uint32_t kb = __ballot_sync(kFull, keep);
             const uint32_t mb = __ballot_sync(kFull, move);
             if (lane == js[t]) {
@@ -609,12 +583,22 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
       }
       stq.flush(S.err);
       stl.flush(S.err);
+      if (kmin != INT_MAX && kmin < *(volatile int32_t *)(s_fmin + lane)) atomicMin(s_fmin + lane, kmin);
+      __syncthreads();
+      // the next advance's minima: what stayed far, and (block 0) the
+      // unchanged minima of the sources that did not advance
+      if (threadIdx.x < kLanes) {
+        int32_t mm = s_fmin[threadIdx.x];
+        if (blockIdx.x == 0 && !((A >> threadIdx.x) & 1u)) mm = min(mm, __ldcg(S.gmin + p * kLanes + threadIdx.x));
+        if (mm != INT_MAX) atomicMin(S.gmin + (p ^ 1) * kLanes + threadIdx.x, mm);
+      }
       if (blockIdx.x == 0 && threadIdx.x < kLanes) S.cur[(p ^ 1) * kLanes + threadIdx.x] = newcur;
+      pending = __ballot_sync(kFull, newcur != INT_MAX) != 0u;
       if (!grid_barrier(S.bar, gridDim.x, S.err, S.timeout_ns)) break;
       ++adv;
     }
     const int32_t m = *(volatile int32_t *)qcnt_out;
-    if (m == 0) break;
+    if (m == 0 && !pending) break;  // an empty window advances again from exact minima
     in ^= 1;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
