@@ -149,6 +149,36 @@ struct WarpStage {
   }
 };
 
+// Final flush of every warp's staged entries with one atomicAdd per CTA: the
+// warps' counts go through shared memory (s_cnt: one int per warp + 1) and
+// thread 0 reserves the CTA's total.  The whole CTA calls it together.
+template <typename T>
+__device__ __forceinline__ void cta_flush(WarpStage<T> &st, int32_t *s_cnt, int32_t *err) {
+  const int32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) s_cnt[w] = st.n;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int32_t tot = 0;
+    for (int32_t i = 0; i < nw; ++i) {
+      const int32_t c = s_cnt[i];
+      s_cnt[i] = tot;
+      tot += c;
+    }
+    s_cnt[nw] = tot ? atomicAdd(st.cnt, tot) : 0;
+  }
+  __syncthreads();
+  const int64_t base = (int64_t)s_cnt[nw] + s_cnt[w];
+  for (int32_t i = lane; i < st.n; i += 32) {
+    if (base + i < st.cap)
+      st.list[base + i] = st.buf[i];
+    else
+      atomicOr(err, DEV_ERR_OVERFLOW);
+  }
+  __syncwarp();
+  st.n = 0;
+  __syncthreads();  // s_cnt is reused by the next flush
+}
+
 // Advances of at most kAdvFew sources walk the far entries with lane = entry:
 // lane l loads the distances of its entry for every advancing source with a
 // far bit there, all at once (instead of 4 entries at a time, lane = source).
@@ -185,15 +215,26 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64
                                          int32_t it, int32_t *wctr, int64_t nwarps, bool scan, int32_t *dl,
                                          int32_t *s_fmin) {
   const int32_t lane = threadIdx.x & 31;
-  for (;;) {
+  // A queue of at most two entries per warp is split statically: no warp
+  // touches the shared counter, whose atomics serialise when thousands of
+  // warps each take one entry (high-diameter graphs run 10^5 such relaxes).
+  const bool fixed = n <= 2 * nwarps;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  for (bool first = true;; first = false) {
     int32_t e0 = 0, B = 1;
-    if (lane == 0) {
-      const int64_t left = n - *(volatile int32_t *)wctr;
-      B = bs_batch(left > 0 ? left / 2 : 1, nwarps);
-      e0 = atomicAdd(wctr, B);
+    if (fixed) {
+      if (!first) break;
+      B = (int32_t)((n + nwarps - 1) / nwarps);
+      e0 = (int32_t)(gw * B < n ? gw * B : n);
+    } else {
+      if (lane == 0) {
+        const int64_t left = n - *(volatile int32_t *)wctr;
+        B = bs_batch(left > 0 ? left / 2 : 1, nwarps);
+        e0 = atomicAdd(wctr, B);
+      }
+      e0 = __shfl_sync(kFull, e0, 0);
+      B = __shfl_sync(kFull, B, 0);
     }
-    e0 = __shfl_sync(kFull, e0, 0);
-    B = __shfl_sync(kFull, B, 0);
     if (e0 >= n) break;
     const int64_t e = (int64_t)e0 + lane;
     int32_t u = 0, b = 0, cnt = 0;
@@ -351,6 +392,7 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64
 __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
   __shared__ int32_t s_cut[kLanes];
   __shared__ int32_t s_fmin[kLanes];  // this CTA's smallest far value per source
+  __shared__ int32_t s_fcnt[256 / 32 + 1];  // cta_flush counts
   // per warp: 32 gathered distance lines (relax), or the staged queue and
   // far-list appends (publish, advance)
   __shared__ alignas(16) int32_t s_wbuf[256 / 32][32 * kLanes];
@@ -422,7 +464,7 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
         }
         stq.push(one, v << 32, S.err);
       }
-      stq.flush(S.err);
+      cta_flush(stq, s_fcnt, S.err);
       act = __reduce_or_sync(kFull, act);
       if (lane == 0 && act) atomicOr(reinterpret_cast<uint32_t *>(S.cnt + 5 + it % 3), act);
     } else {
@@ -581,8 +623,8 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
         }
         stq.push(one, (int64_t)vl << 32, S.err);
       }
-      stq.flush(S.err);
-      stl.flush(S.err);
+      cta_flush(stq, s_fcnt, S.err);
+      cta_flush(stl, s_fcnt, S.err);
       if (kmin != INT_MAX && kmin < *(volatile int32_t *)(s_fmin + lane)) atomicMin(s_fmin + lane, kmin);
       __syncthreads();
       // the next advance's minima: what stayed far, and (block 0) the
