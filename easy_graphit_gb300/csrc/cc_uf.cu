@@ -5,8 +5,9 @@
 //
 //   init     parent[v] = min(v, first neighbour of v)  (adjacency lists are
 //            sorted, so that is v's smallest neighbour)
-//   sample   union(v, first neighbour of v) -- init only covered a smaller one --
-//            and union(v, second neighbour of v); compress every vertex to its root
+//   sample   compress init's chains; union(v, first neighbour of v) where that
+//            neighbour is larger (init joined a smaller one) and union(v, second
+//            neighbour of v); compress every vertex to its root
 //   giant    c = the most frequent root among 1,024 spread-out vertices
 //   finish   every vertex whose root is not c unions with the rest of its
 //            neighbours -- out-neighbours after the two sampled ones and, on a
@@ -70,7 +71,7 @@ __global__ void k_uf_sample(const int32_t *__restrict__ off, const int32_t *__re
     const int32_t b = off[v];
     if (off[v + 1] - b > r) {
       const int32_t u = dst[b + r];
-      if (u != v) uf_union(parent, v, u);
+      if (u != v && (r > 0 || u > v)) uf_union(parent, v, u);  // init joined a smaller first one
     }
   }
 }
@@ -136,7 +137,10 @@ gg_status cc_union_find(gg_graph *g, int32_t *labels, int32_t *parent) {
   const int grid = g->sm_count * 8;
   note_launch();
   k_uf_init<<<grid, 256, 0, st>>>(f.off, f.dst, V, parent);
-  for (int32_t r = 0; r < 2; ++r) {  // init hooked v under a smaller first neighbour only
+  // flatten init's first-neighbour chains before the unions walk them
+  note_launch();
+  k_uf_compress<<<grid, 256, 0, st>>>(parent, V);
+  for (int32_t r = 0; r < 2; ++r) {
     note_launch();
     k_uf_sample<<<grid, 256, 0, st>>>(f.off, f.dst, V, r, parent);
   }
