@@ -279,3 +279,44 @@ def test_multigraph_plan_is_one_captured_launch(app):
         out.fill_(-7)
     plan.close()
     g.close()
+
+
+@pytest.mark.parametrize("delta", [1, 10, 1000])
+def test_sssp_batch_window_from_a_settled_far_value(delta):
+    """0 -> 1 costs 100 (far), but 0 -> 2 -> 1 costs 2: vertex 1's far value 100
+    is the smallest one recorded when source 0 advances, though 1 was settled at
+    2 meanwhile.  The window then starts at 100 and holds nothing; the next
+    advance must still reach 3 (202).  Sources 4 (isolated) and a duplicate of 0
+    ride along."""
+    u = np.array([0, 0, 2, 1], dtype=np.int32)
+    v = np.array([1, 2, 1, 3], dtype=np.int32)
+    w = np.array([100, 1, 1, 200], dtype=np.int32)
+    hg = HostGraph.from_edges(5, u, v, w)
+    g = GraphT(hg)
+    off, dst, ww = np.array(hg.offsets), np.array(hg.dst), np.array(hg.weights)
+    srcs = [0, 4, 0, 2]
+    dist, _ = sssp_batch(g, srcs, delta)
+    np.testing.assert_array_equal(dist[0], [0, 2, 1, 202, INT_MAX])
+    for i, s in enumerate(srcs):
+        np.testing.assert_array_equal(dist[i], oracle.sssp_dijkstra(off, dst, ww, s))
+    g.close()
+
+
+@pytest.mark.parametrize("delta", [4, 64])
+def test_sssp_batch_light_and_heavy_edges(delta):
+    """Weights 1 or 1000 on a random graph: far values recorded through heavy
+    edges are often undercut later through chains of light ones."""
+    rng = np.random.default_rng(3)
+    n, m = 20000, 160000
+    u = rng.integers(0, n, m).astype(np.int32)
+    v = rng.integers(0, n, m).astype(np.int32)
+    w = np.where(rng.random(m) < 0.5, 1, 1000).astype(np.int32)
+    hg = HostGraph.from_edges(n, u, v, w)
+    g = GraphT(hg)
+    off, dst, ww = np.array(hg.offsets), np.array(hg.dst), np.array(hg.weights)
+    srcs = hg.pick_sources(32, seed=9)
+    dist, _ = sssp_batch(g, srcs, delta)
+    for i, s in enumerate(srcs):
+        np.testing.assert_array_equal(dist[i], oracle.sssp_dijkstra(off, dst, ww, int(s)),
+                                      err_msg=f"source {s}")
+    g.close()
