@@ -13,6 +13,11 @@ vertex's out-edges once per source (E_r).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
   torchrun ... bench.py --gpus N     (one rank per GPU; sources shard by rank)
 
+Beside the headline the line carries the per-app comparisons on the same graph
+(`apps`), the delta sweep on it and on the 4096 x 4096 grid (`sssp_sweep`), and
+the other workloads at their own sizes (`other_configs`: BFS on the symmetrized
+R-MAT 16, PageRank on R-MAT 24, CC on the symmetrized R-MAT 24).
+
 The default arm runs the engine (libgg.so) through its C ABI; `--impl
 reference` times the reference's CPU delta-stepping (GAPBS
 OrderedProcessingOperatorNoMerge, as ported in oracle/) on the host cores.
@@ -58,6 +63,9 @@ def parse():
                    help="omit the per-app comparison lines (BFS, BC, PageRank)")
     p.add_argument("--no-sweep", action="store_true",
                    help="omit the delta sweep on this graph and the 4096 x 4096 grid")
+    p.add_argument("--no-configs", action="store_true",
+                   help="omit the lines at the other configurations' own sizes (BFS on the "
+                        "symmetrized R-MAT 16, PageRank on R-MAT 24, CC on the symmetrized R-MAT 24)")
     return p.parse_args()
 
 
@@ -351,6 +359,7 @@ def run_gb300(args):
 
     apps = None if args.no_apps else per_app(g, hg, off, dst, dev, stream, peaks()[0])
     sweep = None if args.no_sweep else delta_sweep(g, h_src, dist_dev, total_edges, dev)
+    other = None if args.no_configs else other_configs(peaks()[0])
 
     if rank != 0:
         if world > 1:
@@ -398,6 +407,7 @@ def run_gb300(args):
         "gpu_launches": launches,
         "apps": apps,
         "sssp_sweep": sweep,
+        "other_configs": other,
     }
     print(json.dumps(out))
     if world > 1:
@@ -465,6 +475,94 @@ def delta_sweep(g, h_src, dist_dev, total_edges, dev):
             "note": "one timed launch per delta on the grid (after an untimed one at delta 128); "
                     "built-in launch shape; CPU: GAPBS OrderedProcessingOperatorNoMerge port, one source, "
                     "all host threads"}
+
+
+def other_configs(peak):
+    """The other workloads at their own sizes, device-timed through the C ABI:
+    BFS on the symmetrized R-MAT 16 from its highest-degree vertex (bfs.cpp's
+    PUSH TWCE fused schedule and the learned selector; the graph fits in L2, so
+    its byte rate is not an HBM figure), PageRank (20 iterations) on the
+    directed R-MAT 24, and CC on the symmetrized R-MAT 24, each against the
+    reference app's own schedule and the OpenMP port on the host cores (CC)."""
+    import oracle
+    from easy_graphit_gb300 import (GraphT, HostGraph, LearnedGPUSchedule, Selector,
+                                    SimpleGPUSchedule as T, bfs, cc, default_schedule, pagerank)
+    threads = os.cpu_count() or 1
+    res = {}
+
+    def best(run, reps=5):
+        out, st = run()
+        for _ in range(reps - 1):
+            o2, s2 = run()
+            if s2["device_ms"] < st["device_ms"]:
+                out, st = o2, s2
+        return out, st
+
+    hg = HostGraph.rmat(16, 16, symmetrize=True)
+    g = GraphT(hg, symmetric=True)
+    off, dst = np.array(hg.offsets), np.array(hg.dst)
+    src = int(np.argmax(np.diff(off)))
+    sch, fz = default_schedule("bfs")
+    def bfs2(*a_):  # (depth, stats)
+        r_ = bfs(*a_)
+        return r_[0], r_[2]
+
+    d, st = best(lambda: bfs2(g, src, sch, fz))
+    ok = bool(np.array_equal(d, oracle.bfs(off, dst, src)))
+    er = int(np.diff(off)[d >= 0].sum())
+    learned = LearnedGPUSchedule(Selector.pretrained())
+    d2, st2 = best(lambda: bfs2(g, src, learned))
+    t0 = time.perf_counter()
+    for _ in range(5):
+        oracle.bfs_omp(off, dst, src, threads)
+    t = (time.perf_counter() - t0) / 5
+    res["bfs_rmat16_symmetrized"] = {
+        "V": hg.num_vertices, "E": hg.num_edges, "source": "highest degree",
+        "plain_gteps": er / st["device_ms"] / 1e6, "learned_gteps": er / st2["device_ms"] / 1e6,
+        "exact": ok and bool(np.array_equal(d2, d)),
+        "cpu_port": {"gteps": er / t / 1e9, "cores": threads, "sample": "OpenMP port of bfs.cpp, mean of 5"},
+        "note": "PUSH TWCE fused (bfs.cpp default); graph L2-resident"}
+    g.close()
+
+    hg = HostGraph.rmat(24, 16)
+    g = GraphT(hg)
+    E, V = hg.num_edges, hg.num_vertices
+    sch, _ = default_schedule("pr")
+    r_plain, st_p = best(lambda: pagerank(g, 20, 0.85, sch), 2)
+    tw = T().configDirection(T.direction_type.PULL).configLoadBalancing(T.load_balancing_type.TWC)
+    r_tw, st_t = best(lambda: pagerank(g, 20, 0.85, tw), 3)
+    gbs = 20 * (8.0 * E + 24.0 * V) / (st_t["device_ms"] / 1e3) / 1e9
+    res["pagerank_rmat24"] = {
+        "V": V, "E": E, "iterations": 20,
+        "plain_gteps": 20 * E / st_p["device_ms"] / 1e6, "static_pull_gteps": 20 * E / st_t["device_ms"] / 1e6,
+        "rel_l1_static_vs_plain": float(np.abs(r_tw.astype(np.float64) - r_plain).sum()
+                                        / np.abs(r_plain.astype(np.float64)).sum()),
+        "roofline": {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                     "bytes_model": "20 x (8 E + 24 V)"},
+        "plain_schedule": "PULL EDGE_ONLY blocked 0x42000 (pr.cpp default)"}
+    g.close()
+    del hg
+
+    hg = HostGraph.rmat(24, 16, symmetrize=True)
+    g = GraphT(hg, symmetric=True)
+    off, dst = np.array(hg.offsets), np.array(hg.dst)
+    E = hg.num_edges
+    sch, _ = default_schedule("cc")
+    lab_r, st_r = best(lambda: cc(g, sch), 2)
+    lab_f, st_f = best(lambda: cc(g, sch, True), 5)
+    t0 = time.perf_counter()
+    lab_c = oracle.cc_omp(off, dst, threads)
+    t = time.perf_counter() - t0
+    res["cc_rmat24_symmetrized"] = {
+        "V": hg.num_vertices, "E": E,
+        "plain_gteps": E / st_r["device_ms"] / 1e6, "fused_gteps": E / st_f["device_ms"] / 1e6,
+        "plain_ms": st_r["device_ms"], "fused_ms": st_f["device_ms"],
+        "exact": bool(np.array_equal(lab_r, lab_f) and np.array_equal(lab_f, lab_c)),
+        "cpu_port": {"gteps": E / t / 1e9, "cores": threads, "sample": "whole run, OpenMP port of cc.cpp"},
+        "plain_schedule": "PUSH EDGE_ONLY rounds (cc.cpp default)",
+        "fused": "union-find in Afforest's sampling order"}
+    g.close()
+    return res
 
 
 def per_app(g, hg, off, dst, dev, stream, peak):
