@@ -357,9 +357,11 @@ def run_gb300(args):
     assert np.array_equal(h_out.numpy(), dd)
     e2e_val, e2e_ms = aggregate_teps(total_edges, e2e_ms, device=dev)
 
-    apps = None if args.no_apps else per_app(g, hg, off, dst, dev, stream, peaks()[0])
-    sweep = None if args.no_sweep else delta_sweep(g, h_src, dist_dev, total_edges, dev)
-    other = None if args.no_configs else other_configs(peaks()[0])
+    # the comparison lines run on rank 0 only (after the timed region)
+    lead = rank == 0
+    apps = per_app(g, hg, off, dst, dev, stream, peaks()[0]) if lead and not args.no_apps else None
+    sweep = delta_sweep(g, h_src, dist_dev, total_edges, dev) if lead and not args.no_sweep else None
+    other = other_configs(peaks()[0]) if lead and not args.no_configs else None
 
     if rank != 0:
         if world > 1:
