@@ -134,12 +134,32 @@ __device__ __forceinline__ void bc_gather(const BcState &st, int32_t v, int32_t 
   }
 }
 
+// Guided hand-out of a phase's work items: a warp takes a batch of up to 32
+// (half of what is left, spread over the warps), so items of very different
+// cost still end the phase together instead of leaving CTAs idle at the grid
+// barrier.  False when none are left; [i0, i1) is the batch.
+__device__ __forceinline__ bool bc_take(int32_t *wc, int32_t ni, int32_t nwarps, int32_t &i0, int32_t &i1) {
+  const int32_t lane = threadIdx.x & 31;
+  int32_t b = 0, B = 1;
+  if (lane == 0) {
+    const int32_t left = ni - *(volatile int32_t *)wc;
+    const int32_t per = left > 0 ? (left / 2 + nwarps - 1) / nwarps : 1;
+    B = per < 1 ? 1 : (per > 32 ? 32 : per);
+    b = atomicAdd(wc, B);
+  }
+  b = __shfl_sync(0xffffffffu, b, 0);
+  B = __shfl_sync(0xffffffffu, B, 0);
+  i0 = b;
+  i1 = min(b + B, ni);
+  return b < ni;
+}
+
 __global__ void __launch_bounds__(512) k_bc_batch(DGraph g, BcState st) {
   extern __shared__ int4 smem[];
   const int32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int32_t nthreads = gridDim.x * blockDim.x;
   const int32_t lane = threadIdx.x & 31;
-  const int32_t gwarp = tid >> 5, nwarps = nthreads >> 5;
+  const int32_t nwarps = nthreads >> 5;
   LoopClock clk;
   clk.start(st.loop_limit_ns);
   bool alive = true;
@@ -162,12 +182,14 @@ __global__ void __launch_bounds__(512) k_bc_batch(DGraph g, BcState st) {
       st.loff[d] = b_d;
       st.loff[d + 1] = e_d;
       st.ctr[1 + (d & 1)] = 0;  // items of Q_{d+1}, filled by the publish below
+      st.ctr[16 + ((d + 1) & 1)] = 0;  // hand-out counter of the next level's gather
     }
     // sigma of Q_d from Q_{d-1} (items made by the previous publish)
     if (d > 0) {
       const int32_t ni = min(*(volatile int32_t *)(st.ctr + 1 + ((d - 1) & 1)), st.wcap);
       const uint64_t *pm = bc_fr(st, d - 1), *nm = bc_fr(st, d);
-      for (int32_t i = gwarp; i < ni; i += nwarps) {
+      for (int32_t i0, i1; bc_take(st.ctr + 16 + (d & 1), ni, nwarps, i0, i1);)
+      for (int32_t i = i0; i < i1; ++i) {
         const int64_t it = __ldcg(st.work + i);
         const int32_t v = (int32_t)(it >> 32), c = (int32_t)(uint32_t)it;
         const uint64_t own = __ldcg(nm + v);
@@ -245,7 +267,10 @@ __global__ void __launch_bounds__(512) k_bc_batch(DGraph g, BcState st) {
   // ------------------------------------------------------------ backward
   for (int32_t dd = L - 1; alive && dd >= 0; --dd) {
     if (stopped(st.stop, st.err)) break;
-    if (tid == 0) st.ctr[3 + ((dd + 1) & 1)] = 0;  // consumed by the gather of level dd + 1
+    if (tid == 0) {
+      st.ctr[3 + ((dd + 1) & 1)] = 0;   // consumed by the gather of level dd + 1
+      st.ctr[18 + ((dd + 1) & 1)] = 0;  // that gather's hand-out counter
+    }
     // sources at level dd + 1 become "deeper" for the gathers from here on
     if (dd + 1 < L) {
       uint64_t *lmo = bc_lm(st, dd + 1);
@@ -288,7 +313,8 @@ __global__ void __launch_bounds__(512) k_bc_batch(DGraph g, BcState st) {
     {
       const int32_t ni = min(*(volatile int32_t *)(st.ctr + 3 + (dd & 1)), st.wcap);
       const uint64_t *lmn = bc_lm(st, dd);
-      for (int32_t i = gwarp; i < ni; i += nwarps) {
+      for (int32_t i0, i1; bc_take(st.ctr + 18 + (dd & 1), ni, nwarps, i0, i1);)
+      for (int32_t i = i0; i < i1; ++i) {
         const int64_t it = __ldcg(st.work + i);
         const int32_t v = (int32_t)(it >> 32), c = (int32_t)(uint32_t)it;
         const uint64_t own = __ldcg(lmn + v);
