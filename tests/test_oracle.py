@@ -148,3 +148,35 @@ def test_shortest_path_certificate_accepts_exact_and_rejects_wrong_distances():
     bad[reached[-1]] += 1                     # too large: an edge improves it
     assert not shortest_paths_certified(off, dst, w, bad, s)
     assert not shortest_paths_certified(off, dst, w, np.zeros_like(d), s)
+
+
+@pytest.mark.parametrize("name", ["rmat10_k16_sym", "rmat12_k16_dir"])
+def test_cc_matches_scipy_weak_components(golden, name):
+    """An independent implementation: scipy's weakly connected components,
+    relabelled to the smallest vertex id of each component (cc.cpp's fixpoint)."""
+    sp = pytest.importorskip("scipy.sparse")
+    csg = pytest.importorskip("scipy.sparse.csgraph")
+    off, dst, _ = _g(golden, name)
+    V = len(off) - 1
+    A = sp.csr_matrix((np.ones(len(dst)), dst, off), shape=(V, V))
+    n, comp = csg.connected_components(A, directed=True, connection="weak")
+    smallest = np.full(n, V, dtype=np.int64)
+    np.minimum.at(smallest, comp, np.arange(V))
+    np.testing.assert_array_equal(oracle.cc(off, dst), smallest[comp])
+
+
+@pytest.mark.parametrize("name", ["rmat10_k16_sym", "rmat12_k16_dir"])
+def test_pagerank_matches_sparse_power_iteration(golden, name):
+    """pr.cpp's iteration written as a sparse matrix product in FP64:
+    new = (1-d)/V + d * A^T (old / outdeg), 20 times, no dangling redistribution
+    (a sink's contribution is never read: it has no out-edges)."""
+    sp = pytest.importorskip("scipy.sparse")
+    off, dst, _ = _g(golden, name)
+    V = len(off) - 1
+    A = sp.csr_matrix((np.ones(len(dst)), dst, off), shape=(V, V))
+    outdeg = np.diff(off).astype(np.float64)
+    r = np.full(V, 1.0 / V)
+    for _ in range(20):
+        contrib = np.divide(r, outdeg, out=np.zeros(V), where=outdeg > 0)
+        r = (1.0 - 0.85) / V + 0.85 * (A.T @ contrib)
+    assert rel_l1(oracle.pagerank(off, dst, 20, 0.85), r) < 1e-12
