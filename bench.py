@@ -420,7 +420,7 @@ def delta_sweep(g, h_src, dist_dev, total_edges, dev):
     """Batched SSSP (32 sources, one launch) over the delta sweep {1, 8, 32, 128}
     on this graph, and on the 4096 x 4096 4-neighbour grid (weights U[1,1000],
     high diameter) at delta 128 and 32 -- there delta 8 and 1 take 3 x 10^5 and
-    more buckets (17 s and more per launch).  Loop time by CUDA events; the
+    more buckets (several seconds and more per launch).  Loop time by CUDA events; the
     GAPBS ordered-processing port on the host cores runs one grid source at the
     same deltas beside it.  All deltas give the same distances (checked)."""
     import ctypes as C
