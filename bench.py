@@ -63,6 +63,9 @@ def parse():
                    help="omit the per-app comparison lines (BFS, BC, PageRank)")
     p.add_argument("--no-sweep", action="store_true",
                    help="omit the delta sweep on this graph and the 4096 x 4096 grid")
+    p.add_argument("--autotune-table", metavar="PATH", default=None,
+                   help="only tabulate the autotuned launch shapes of the batched kernels per graph size "
+                        "(R-MAT 12-22, grids 256-2048) as markdown into PATH, then exit")
     p.add_argument("--no-configs", action="store_true",
                    help="omit the lines at the other configurations' own sizes (BFS on the "
                         "symmetrized R-MAT 16, PageRank on R-MAT 24, CC on the symmetrized R-MAT 24)")
@@ -79,6 +82,16 @@ def dist_env():
 def make_graph(scale):
     from easy_graphit_gb300 import HostGraph
     return HostGraph.rmat(scale, DEGREE)
+
+
+def bench_config(scale, V, E, delta):
+    """The workload, the same in both arms."""
+    return {"workload": f"sssp_delta_stepping_rmat{scale}_k16_directed", "V": int(V), "E": int(E),
+            "sources": N_SOURCES, "delta": int(delta), "weights": "U[1,255]",
+            "graph": "R-MAT a/b/c 0.57/0.19/0.19, GAPBS generator and builder, seed 27491095; "
+                     "sources from GAPBS SourcePicker",
+            "l2": "inputs larger than L2 (CSR %.2f GB, distances %.2f GB)"
+                  % ((4.0 * (V + 1) + 8.0 * E) / 1e9, N_SOURCES * V * 4 / 1e9)}
 
 
 def reached_stats(off, dist):
@@ -185,12 +198,16 @@ def ncu_traffic():
 
 # ------------------------------------------------------------------- arms
 def run_reference(args):
+    """The reference's CPU SSSP (GAPBS OrderedProcessingOperatorNoMerge, as
+    ported in the oracle) on the host cores, over a graph the oracle builds
+    itself (its restatement of GAPBS's generator): no engine code is loaded."""
     rank, world, _ = dist_env()
     if world > 1 and rank != 0:
         return
-    hg = make_graph(args.scale)
-    off, dst, w = np.array(hg.offsets), np.array(hg.dst), np.array(hg.weights)
-    sources = hg.pick_sources(N_SOURCES)
+    import oracle
+    off, dst, w = oracle.rmat(args.scale, DEGREE)
+    V, E = len(off) - 1, len(dst)
+    sources = oracle.pick_sources(off, N_SOURCES)
     delta = args.delta or 32
     per_step = 2  # bounded sample of the 32 sources per step
     vals = []
@@ -205,8 +222,7 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic",
-        "config": {"workload": f"sssp_delta_stepping_rmat{args.scale}_k16_directed",
-                   "sources": N_SOURCES, "delta": delta, "weights": "U[1,255]"},
+        "config": bench_config(args.scale, V, E, delta),
         "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": threads, "kind": "port",
                          "sample": f"{per_step} of the {N_SOURCES} sources per step "
                                    f"(GAPBS OrderedProcessingOperatorNoMerge port, all host threads)"},
@@ -381,22 +397,19 @@ def run_gb300(args):
         "metric": METRIC, "value": value, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": f"sssp_delta_stepping_rmat{args.scale}_k16_directed",
-                   "V": V, "E": E, "sources": N_SOURCES, "delta": delta,
-                   "delta_sweep": list(DELTAS), "weights": "U[1,255]",
-                   "mode": "batched: 32 sources per persistent launch (gg_sssp_batch)",
-                   "plain_gteps": plain_gteps,
-                   "plain_schedule": "PUSH SPARSE VERTEX_BASED fused, one source at a time (sssp.cpp default)",
-                   "single_twce_gteps": twce_gteps,
-                   "single_learned_gteps": learned_gteps,
-                   "learned_schedule": "LearnedGPUSchedule(Selector.pretrained()), unfused, one source at a time",
-                   "batch_tuning": tuned if tuned else "built-in (blocks_per_sm all that fit, chunk 256, "
-                                                        "edge_parallel_max 6)",
-                   "autotune_trials": len(tune_rows),
-                   "batched_over_plain": value / world / plain_gteps,
-                   "l2": "inputs larger than L2 (CSR %.2f GB, distances %.2f GB)"
-                   % ((off.nbytes + dst.nbytes + w.nbytes) / 1e9, N_SOURCES * V * 4 / 1e9),
-                   "parallelism": f"replicas x{world}, sources by rank"},
+        "config": bench_config(args.scale, V, E, delta),
+        "comparisons": {"delta_sweep": list(DELTAS),
+                        "mode": "batched: 32 sources per persistent launch (gg_sssp_batch)",
+                        "plain_gteps": plain_gteps,
+                        "plain_schedule": "PUSH SPARSE VERTEX_BASED fused, one source at a time (sssp.cpp default)",
+                        "single_twce_gteps": twce_gteps,
+                        "single_learned_gteps": learned_gteps,
+                        "learned_schedule": "LearnedGPUSchedule(Selector.pretrained()), unfused, one source at a time",
+                        "batch_tuning": tuned if tuned else "built-in (blocks_per_sm all that fit, chunk 256, "
+                                                             "edge_parallel_max 6)",
+                        "autotune_trials": len(tune_rows),
+                        "batched_over_plain": value / world / plain_gteps,
+                        "parallelism": f"replicas x{world}, sources by rank"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": "k_bsssp", "peak_kind": peak_kind,
@@ -671,8 +684,47 @@ def per_app(g, hg, off, dst, dev, stream, peak):
     return res
 
 
+def autotune_table(path, delta=32):
+    """gg_batch_autotune for batched BFS (64 sources), SSSP (32 sources) and BC
+    (64 sources) on R-MAT graphs of scale 12 to 22 (edge factor 16; BC and grids
+    symmetric) and grids of side 256 to 2048: the chosen CTAs per SM, chunk,
+    edge-parallel threshold and bottom-up divisor, with the tuned and built-in
+    launch shapes' times (CUDA events around one persistent launch)."""
+    from easy_graphit_gb300 import GraphT, HostGraph, autotune_batch, set_batch_tuning
+    sizes = [("rmat", 12), ("rmat", 14), ("rmat", 16), ("rmat", 18), ("rmat", 20), ("rmat", 22),
+             ("grid", 256), ("grid", 1024), ("grid", 2048)]
+    apps = [("bfs", 64), ("sssp", 32), ("bc", 64)]
+    lines = ["| graph | V | E | app | sources | CTAs/SM | chunk | edge-parallel max | bottom-up div | "
+             "tuned ms | built-in ms | trials |", "|---|---|---|---|---|---|---|---|---|---|---|---|"]
+    t0 = time.time()
+    for kind, size in sizes:
+        for app, nsrc in apps:
+            sym = app == "bc" or kind == "grid"
+            hg = HostGraph.rmat(size, 16, symmetrize=sym) if kind == "rmat" else HostGraph.grid(size, size)
+            g = GraphT(hg, symmetric=sym)
+            best, rows = autotune_batch(g, app, hg.pick_sources(nsrc), delta)
+            fit = max(t["blocks_per_sm"] for t, _ in rows)
+            ms = min(m for t, m in rows if t == best)
+            base = next((m for t, m in rows if t["blocks_per_sm"] == fit and t["chunk"] in (0, 256)
+                         and t["edge_parallel_max"] in (0, 6) and t["bottom_up_div"] in (0, 16)), None)
+            name = (f"R-MAT {size}{' sym' if sym else ''}" if kind == "rmat" else f"grid {size}x{size}")
+            lines.append(f"| {name} | {hg.num_vertices} | {hg.num_edges} | {app} | {nsrc} | "
+                         f"{best['blocks_per_sm']} | {best['chunk'] if app != 'bfs' else '-'} | "
+                         f"{best['edge_parallel_max'] if app == 'sssp' else '-'} | "
+                         f"{best['bottom_up_div'] if app == 'bfs' else '-'} | {ms:.3f} | "
+                         f"{'-' if base is None else f'{base:.3f}'} | {len(rows)} |")
+            print(lines[-1], flush=True)
+            set_batch_tuning(g, app)
+            g.close()
+    text = "\n".join(lines) + f"\n\n({time.time() - t0:.0f} s; delta {delta} for SSSP)\n"
+    Path(path).write_text(text)
+
+
 def main():
     args = parse()
+    if args.autotune_table:
+        autotune_table(args.autotune_table)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

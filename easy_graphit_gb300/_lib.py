@@ -82,6 +82,7 @@ SIGNATURES: dict[str, tuple] = {
     "gg_host_graph_from_csr": (i32, [i32, i64, P, P, P, C.POINTER(P)]),
     "gg_host_graph_load": (i32, [C.c_char_p, i32, C.POINTER(P)]),
     "gg_host_graph_save_bin": (i32, [P, C.c_char_p]),
+    "gg_host_graph_save_sg": (i32, [P, C.c_char_p, i32]),
     "gg_host_graph_info": (i32, [P, Pi32, C.POINTER(i64)]),
     "gg_host_graph_pick_sources": (i32, [P, i32, i64, P]),
     "gg_host_graph_offsets": (P, [P]),

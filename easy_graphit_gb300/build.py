@@ -100,12 +100,12 @@ def build_oracle() -> Path:
 
 
 def build_ref_oracle() -> Path | None:
-    """Compiles the reference's GAPBS code into oracle/_ref when the reference
-    tree is present (it is not on machines that only run the tests)."""
-    ref = Path(os.environ.get("GG_REF_DIR", "/root/reference"))
-    if not (ref / "runtime" / "infra_gapbs").is_dir():
+    """Compiles the reference's GAPBS code into oracle/_ref when GG_REF_DIR names
+    a reference tree (machines that only run the tests have none)."""
+    ref_dir = os.environ.get("GG_REF_DIR")
+    if not ref_dir or not (Path(ref_dir) / "runtime" / "infra_gapbs").is_dir():
         return None
-    _run(["make", "-s", "-C", str(ORACLE), "ref", f"REF_DIR={ref}"])
+    _run(["make", "-s", "-C", str(ORACLE), "ref", f"REF_DIR={ref_dir}"])
     return ORACLE / "_ref" / "ref_gapbs"
 
 

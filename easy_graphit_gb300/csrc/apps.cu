@@ -275,7 +275,7 @@ gg_status run_sssp(gg_graph *g, const gg_app_schedule *s, const int32_t *srcs, i
     bool ran = false;
     int32_t iters = 0;
     int64_t adv = 0;
-    GG_TRY(fused_sssp(g, &s->s1, nsrc, delta, vd, pq->frontier, &iters, &adv, &ran));
+    GG_TRY(fused_sssp(g, &s->s1, nsrc, delta, vd, pq, &iters, &adv, &ran));
     if (ran) {
       if (st) {
         st->iterations = iters;
@@ -297,6 +297,7 @@ gg_status run_sssp(gg_graph *g, const gg_app_schedule *s, const int32_t *srcs, i
     GG_TRY(frontier_size(pq->frontier, &n));
     const gg_schedule *sc = nullptr;
     GG_TRY(ch.choose(pq->frontier, n, &sc));
+    vd.far = pq_far(pq);
     GG_TRY(edgeset_apply_impl(g, sc, GG_UDF_SSSP_RELAX, GG_FILTER_NONE, pq->frontier, pq->frontier,
                               true, vd, pq_cutoff(pq), false));
     if (st) st->iterations++;

@@ -18,6 +18,7 @@ struct gg_batch_plan {
   gg::MsBfsBuffers ms;
   gg::BcBuffers bc;
   int32_t *parent = nullptr;              // BFS multi-source: parent scratch
+  gg::BqBuffers bq;                       // SSSP multi-source: bucket-queue buffers
   unsigned long long *reached = nullptr;  // BC: reached out-edges summed over sources
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -29,6 +30,7 @@ struct gg_batch_plan {
     if (dstats) cudaFree(dstats);
     if (reached) cudaFree(reached);
     if (parent) cudaFree(parent);
+    if (bq.base) gg::bq_free(g, &bq);
   }
 };
 
@@ -60,6 +62,7 @@ gg_status gg_batch_plan_create(gg_graph *g, int32_t app, const int32_t *sources,
   if (multi) {
     if (!g->app_frontier) GG_TRY(gg_frontier_create(g, 0, &g->app_frontier));
     if (app == GG_BATCH_BFS_MULTI) GG_CUDA(cudaMalloc(&p->parent, sizeof(int32_t) * std::max(V, 1)));
+    if (app == GG_BATCH_SSSP_MULTI) GG_TRY(bq_alloc(g, &p->bq));
   } else if (app == GG_BATCH_BFS) {
     GG_TRY(msbfs_buffers(g, nsrc, true, &p->ms));
   } else if (app == GG_BATCH_SSSP) {
@@ -80,9 +83,11 @@ gg_status gg_batch_plan_create(gg_graph *g, int32_t app, const int32_t *sources,
     if (me != cudaSuccess) st = set_error(GG_ERR_CUDA, "memset in capture: %s", cudaGetErrorString(me));
   }
   if (multi) {
-    st = fused_multi_enqueue(g, cs, app == GG_BATCH_SSSP_MULTI, p->dsrc, nsrc, delta, p->parent, (int32_t *)out);
+    const int32_t *run_stats = nullptr;
+    st = fused_multi_enqueue(g, cs, app == GG_BATCH_SSSP_MULTI, p->dsrc, nsrc, delta, p->parent, (int32_t *)out,
+                             &p->bq, &run_stats);
     if (st == GG_OK) {
-      const cudaError_t ce2 = cudaMemcpyAsync(p->dstats, g->d_misc + 44, sizeof(int32_t) * 2,
+      const cudaError_t ce2 = cudaMemcpyAsync(p->dstats, run_stats, sizeof(int32_t) * 2,
                                               cudaMemcpyDeviceToDevice, cs);
       if (ce2 != cudaSuccess) st = set_error(GG_ERR_CUDA, "stats copy in capture: %s", cudaGetErrorString(ce2));
     }

@@ -142,6 +142,41 @@ struct DOut {
   }
 };
 
+// Far piles of the single-source delta-stepping queue (bucket_queue.cuh).  A
+// relaxation that lowers P[v] to p at or above the window's cutoff parks v on
+// the low pile (p below the horizon) or the high pile.  stamp[v] holds the tag
+// of the pile generation that already lists v, so each vertex is listed at most
+// once per pile: the exchange that writes the tag decides who appends.  With
+// stamp == nullptr nothing is parked (a plain edgeset.apply of the relax UDF).
+struct DFar {
+  int32_t *stamp;           // [V]
+  int32_t *lo, *lo_cnt;     // low pile of the current generation and its count
+  int32_t *hi, *hi_cnt;     // high pile of the current generation and its count
+  int32_t lo_tag, hi_tag;
+  int32_t horizon;          // p < horizon -> low pile
+  int32_t cap;              // entries a pile can hold (V)
+  int32_t *err;
+
+  __device__ __forceinline__ void park(int32_t v, int32_t p) const {
+    const bool low = p < horizon;
+    const int32_t tag = low ? lo_tag : hi_tag;
+    if (*(volatile int32_t *)(stamp + v) == tag || atomicExch(stamp + v, tag) == tag) return;
+    if (low) {
+      const int32_t pos = agg_inc(lo_cnt);
+      if (pos < cap)
+        lo[pos] = v;
+      else
+        atomicOr(err, DEV_ERR_OVERFLOW);
+    } else {
+      const int32_t pos = agg_inc(hi_cnt);
+      if (pos < cap)
+        hi[pos] = v;
+      else
+        atomicOr(err, DEV_ERR_OVERFLOW);
+    }
+  }
+};
+
 // --------------------------------------------------------------- barriers
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
   uint32_t v;
@@ -192,6 +227,34 @@ __device__ __forceinline__ bool grid_barrier(uint32_t *bar, uint32_t nblocks, in
   }
   __syncthreads();
   return ok_s != 0;
+}
+
+// Waits, without arriving, until every other block has arrived at the next
+// grid_barrier (bar[0] counts arrivals and the previous barrier's last block
+// reset it, so nblocks-1 arrivals means all others are inside the wait).  The
+// caller then works alone and completes the barrier by calling grid_barrier
+// itself.  Bounded like grid_barrier; false after the limit.
+__device__ __forceinline__ bool grid_wait_others(const uint32_t *bar, uint32_t nblocks, int32_t *err,
+                                                 uint64_t timeout_ns) {
+  __shared__ int ok_o;
+  if (threadIdx.x == 0) {
+    ok_o = 1;
+    const uint64_t t0 = globaltimer_ns();
+    uint32_t spins = 0;
+    while (ld_acquire(bar) < nblocks - 1) {
+      if ((++spins & 255u) == 0) {
+        if (*(volatile int32_t *)err & DEV_ERR_TIMEOUT) { ok_o = 0; break; }
+        if (globaltimer_ns() - t0 > timeout_ns) {
+          atomicOr(err, DEV_ERR_TIMEOUT);
+          ok_o = 0;
+          break;
+        }
+      }
+      __nanosleep(32);
+    }
+  }
+  __syncthreads();
+  return ok_o != 0;
 }
 
 // Wall-clock bound of a persistent loop.  Block 0 raises *stop just before an

@@ -5,7 +5,7 @@
 namespace gg {
 
 gg_status launch_sssp(const EdgeLaunch &L) {
-  USssp u{L.vd.dist, L.prio_cutoff};
+  USssp u{L.vd.dist, L.prio_cutoff, L.vd.far};
   return launch_dir(L, u);
 }
 

@@ -8,6 +8,7 @@
 #include <memory>
 #include <vector>
 
+#include "bucket_queue.cuh"
 #include "common.cuh"
 
 namespace gg {
@@ -89,6 +90,10 @@ struct gg_pq {
   bool ready_set_dequeued = false;
   gg_frontier *frontier = nullptr; // frontier_
   int64_t advances = 0;
+  gg::BqBuffers bq;                // far piles (bucket_queue.cuh), also used by the fused loop
+  int32_t gen_lo = 0, gen_hi = 0;  // pile generations of the host-driven queue
+  int32_t horizon = INT_MAX;
+  int32_t width = 16;              // horizon width in buckets
 };
 
 struct gg_frontier_list {
@@ -110,6 +115,7 @@ struct VData {
   uint8_t *visited;
   int32_t level, src;
   float damping;
+  DFar far;  // far piles of the delta-stepping queue (read by the relax UDF only)
 };
 VData to_vdata(const gg_vertex_data *vd);
 
@@ -189,6 +195,7 @@ gg_status pq_finished(gg_pq *pq, bool *fin);
 gg_status pq_dequeue(gg_pq *pq);
 gg_status pq_reset(gg_pq *pq, int32_t init_priority, int32_t delta, int32_t src);
 int32_t pq_cutoff(const gg_pq *pq);
+DFar pq_far(const gg_pq *pq);  // far piles the relax parks into
 
 // ---- fused.cu: whole-loop persistent kernels (fuse_kernel, operators.cpp:652-672).
 // *ran is false when the schedule has no device-side form (the caller then
@@ -196,12 +203,20 @@ int32_t pq_cutoff(const gg_pq *pq);
 bool fused_supported(const gg_schedule *s);
 // Multi-source BFS (depth, parent scratch) or SSSP (dist) with the TWCE fused
 // loop, every step on the device (capturable); sources in device memory.
+// SSSP uses the bucket-queue buffers *bq; *stats receives the device address of
+// the run's {iterations, bucket advances}.
 gg_status fused_multi_enqueue(gg_graph *g, cudaStream_t st, bool sssp, const int32_t *dsrc, int32_t n,
-                              int32_t delta, int32_t *parent, int32_t *out);
+                              int32_t delta, int32_t *parent, int32_t *out, const BqBuffers *bq,
+                              const int32_t **stats);
 gg_status fused_bfs(gg_graph *g, const gg_schedule *s, int32_t n0, const VData &vd,
                     gg_frontier *f, int32_t *iters, bool *ran);
 gg_status fused_sssp(gg_graph *g, const gg_schedule *s, int32_t n0, int32_t delta, const VData &vd,
-                     gg_frontier *f, int32_t *iters, int64_t *advances, bool *ran);
+                     gg_pq *pq, int32_t *iters, int64_t *advances, bool *ran);
+// Bucket-queue buffers for V vertices (pool memory on the graph's stream), their
+// release, and the reset at the start of a run with n0 sources on the frontier.
+gg_status bq_alloc(gg_graph *g, BqBuffers *b);
+void bq_free(gg_graph *g, BqBuffers *b);
+gg_status bq_start(const BqBuffers &b, int32_t n0, cudaStream_t st);
 uint64_t barrier_timeout_ns();
 uint64_t loop_timeout_ns();  // wall-clock bound of one persistent loop (GG_LOOP_TIMEOUT_MS)
 

@@ -322,6 +322,13 @@ gg_status frontier_size(gg_frontier *f, int32_t *n) {
   GG_CUDA(cudaMemcpyAsync(g->h_pinned, f->cnt_in, sizeof(int32_t), cudaMemcpyDeviceToHost, g->stream));
   GG_CUDA(cudaStreamSynchronize(g->stream));
   *n = g->h_pinned[0];
+  if (*n > f->cap) {
+    // enqueues past the capacity were dropped (and flagged); a count this
+    // large must never bound a loop over the queue
+    *n = 0;
+    GG_TRY(check_device_error(g, "frontier"));
+    return set_error(GG_ERR_OVERFLOW, "frontier queue capacity exceeded");
+  }
   return GG_OK;
 }
 

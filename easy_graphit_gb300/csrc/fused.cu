@@ -9,6 +9,7 @@
 // finished before the previous barrier -- one barrier per iteration.
 #include <cstdlib>
 
+#include "bucket_queue.cuh"
 #include "engine.h"
 #include "lb.cuh"
 #include "udf.cuh"
@@ -46,22 +47,24 @@ bool fused_supported(const gg_schedule *s) {
   }
 }
 
+// Runs one LB strategy over the n enumerated vertices; CTA `rank` of `nparts`
+// takes every nparts-th virtual CTA (nparts = 1: one CTA does all of it).
 template <int LB, class F>
 __device__ __forceinline__ void run_lb(const DGraph &g, const Enum &en, int32_t n, const F &f,
-                                       const DOut &out, int4 *smem) {
+                                       const DOut &out, int4 *smem, int32_t rank, int32_t nparts) {
   if (LB == GG_LB_VERTEX_BASED) {
     const int32_t nv = ceil_div(n, blockDim.x);
-    for (int32_t v = blockIdx.x; v < nv; v += gridDim.x) lb_vertex(g, en, n, f, out, v);
+    for (int32_t v = rank; v < nv; v += nparts) lb_vertex(g, en, n, f, out, v);
   } else if (LB == GG_LB_WM) {
     const int32_t nv = ceil_div(n, blockDim.x >> 5);
-    for (int32_t v = blockIdx.x; v < nv; v += gridDim.x) lb_wm(g, en, n, f, out, v);
+    for (int32_t v = rank; v < nv; v += nparts) lb_wm(g, en, n, f, out, v);
   } else if (LB == GG_LB_TWCE) {
     const int32_t nv = ceil_div(n, blockDim.x / kStage1);
-    for (int32_t v = blockIdx.x; v < nv; v += gridDim.x)
+    for (int32_t v = rank; v < nv; v += nparts)
       lb_twce<F, true>(g, en, n, f, out, v, *reinterpret_cast<TwceSmem *>(smem));
   } else {
     const int32_t nv = ceil_div(n, blockDim.x);
-    for (int32_t v = blockIdx.x; v < nv; v += gridDim.x)
+    for (int32_t v = rank; v < nv; v += nparts)
       lb_cm(g, en, n, f, out, v, *reinterpret_cast<CmSmem *>(smem));
   }
 }
@@ -107,7 +110,7 @@ __global__ void __launch_bounds__(1024) k_bfs_fused(FusedArgs a) {
     const Enum en{qs[in], nullptr, n};
     const EdgeF<UBfs, false> f{UBfs{a.vd.parent, a.vd.depth, (int32_t)level},
                                DIn{IN_ALL, nullptr, nullptr}, DIn{IN_ALL, nullptr, nullptr}, true};
-    run_lb<LB>(a.g, en, n, f, sparse_out(a, qs[in ^ 1], level), smem);
+    run_lb<LB>(a.g, en, n, f, sparse_out(a, qs[in ^ 1], level), smem, blockIdx.x, gridDim.x);
     clk.tick(a.stop);
     if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
     in ^= 1;
@@ -115,87 +118,288 @@ __global__ void __launch_bounds__(1024) k_bfs_fused(FusedArgs a) {
   if (blockIdx.x == 0 && threadIdx.x == 0) a.stats[0] = (int32_t)(level - 1);
 }
 
-// Delta-stepping with the GPUPriorityQueue semantics of gpu_priority_queue.h:
-// relax the frontier with cutoff cur+delta; when it runs empty, advance cur to
-// the smallest priority >= cur+delta and enqueue [cur, cur+delta).
-template <int LB>
-__global__ void __launch_bounds__(1024) k_sssp_fused(FusedArgs a) {
-  extern __shared__ int4 smem[];
-  __shared__ int32_t wmin[32];
-  int32_t *qs[2] = {a.q0, a.q1};
-  const int32_t V = a.g.V;
-  int in = 0;
-  int64_t it = 1, cur = 0, adv = 0, relax = 0;
-  LoopClock clk;
-  clk.start(a.loop_limit_ns);
-  for (;; ++it) {
-    const int32_t n = *(volatile int32_t *)(a.cnt3 + (it - 1) % 3);
-    if (stopped(a.stop, a.err)) break;
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.cnt3[(it + 1) % 3] = 0;
-    if (n == 0) {
-      const int64_t window = cur + a.delta;
-      int32_t *gm = a.gmin2 + (adv & 1);
-      if (blockIdx.x == 0 && threadIdx.x == 0) a.gmin2[(adv + 1) & 1] = INT_MAX;
-      int32_t m = INT_MAX;
-      if (window < INT_MAX)
-        for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-          const int32_t p = a.vd.dist[v];
-          if (p >= window && p != INT_MAX && p < m) m = p;
-        }
-#pragma unroll
-      for (int d = 16; d > 0; d >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, d));
-      if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = m;
-      __syncthreads();
-      if (threadIdx.x < 32) {
-        m = threadIdx.x < (blockDim.x >> 5) ? wmin[threadIdx.x] : INT_MAX;
-#pragma unroll
-        for (int d = 16; d > 0; d >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, d));
-        if (threadIdx.x == 0 && m != INT_MAX) atomicMin(gm, m);
-      }
-      if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
-      cur = *(volatile int32_t *)gm;
-      ++adv;
-      if (cur == INT_MAX) break;
-      const int64_t hi = cur + a.delta;
-      int32_t *qo = qs[in ^ 1];
-      int32_t *cnt = a.cnt3 + it % 3;
-      const int32_t stride = gridDim.x * blockDim.x;
-      for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < ceil_div(V, stride) * stride;
-           v += stride) {
-        bool p = false;
-        if (v < V) {
-          const int32_t x = a.vd.dist[v];
-          p = x >= cur && (int64_t)x < hi;
-        }
-        const uint32_t mk = __ballot_sync(0xffffffffu, p);
-        if (mk) {
-          const int32_t lane = threadIdx.x & 31;
-          int32_t base = 0;
-          if (lane == 0) base = atomicAdd(cnt, __popc(mk));
-          base = __shfl_sync(0xffffffffu, base, 0);
-          if (p) qo[base + __popc(mk & ((1u << lane) - 1))] = v;
-        }
-      }
-    } else {
-      const int64_t c = cur + a.delta;
-      const Enum en{qs[in], nullptr, n};
-      const EdgeF<USssp, false> f{USssp{a.vd.dist, c > INT_MAX ? INT_MAX : (int32_t)c},
-                                  DIn{IN_ALL, nullptr, nullptr}, DIn{IN_ALL, nullptr, nullptr}, false};
-      run_lb<LB>(a.g, en, n, f, sparse_out(a, qs[in ^ 1], it), smem);
-      ++relax;
+// ------------------------------------------------------ delta-stepping SSSP
+// The sssp.cpp loop (apps/sssp.cpp:47-52) fused into one persistent kernel
+// over the bucket queue of bucket_queue.cuh.  Each step is one of
+//   relax     the frontier with cutoff cur+delta (improvements below it queue
+//             the vertex, the others park it on a far pile),
+//   lo-min    exact minimum of the low pile's live entries,
+//   lo-split  window entries to the frontier, the rest to the next low pile,
+//   hi-min / hi-split  the same over the high pile when the low pile holds
+//             nothing live (a refill, which also sets the next horizon),
+// and ends at a grid barrier.  Frontier counts and minima rotate through
+// three slots: a step clears the slot two steps ahead, whose readers finished
+// before the previous barrier.
+//
+// One-CTA mode: a step whose work (frontier or pile entries) is at most
+// solo_max runs on CTA 0 alone, and so do the steps after it while they stay
+// that small, separated by __syncthreads; the other CTAs wait at the grid
+// barrier.  CTA 0 begins only when all of them have arrived there: its first
+// steps clear control words that a slower CTA could otherwise still be
+// reading to take the same decision.  CTA 0 returns to the barrier when the work grows, the loop ends or
+// kSoloSliceNs has passed (so the waiting CTAs see a barrier complete at least
+// that often), and publishes the loop state for the others.  Small buckets --
+// a 4096^2 grid at delta 1 has 1.3 M of them, 13 vertices each on average --
+// then cost a few L2 round trips instead of three grid barriers.
+enum : int32_t { BQ_RELAX = 0, BQ_LOMIN = 1, BQ_LOSPLIT = 2, BQ_HIMIN = 3, BQ_HISPLIT = 4, BQ_DONE = 5 };
+constexpr uint64_t kSoloSliceNs = 1000000;
+
+struct BqArgs {
+  DGraph g;
+  int32_t *q0, *q1;  // frontier queues
+  int64_t qcap;
+  int32_t *dist;
+  BqBuffers b;       // stamps, piles, control words
+  uint32_t *bar;
+  int32_t *err;
+  uint64_t timeout_ns, loop_limit_ns;
+  int32_t delta;
+  int32_t solo_max;     // largest step CTA 0 runs alone
+  int32_t fill_target;  // low-pile entries a refill aims for
+  int32_t width0;       // first horizon width, in buckets
+};
+
+// Loop state, the same in every CTA: every decision is taken from control
+// words read after a barrier.
+struct BqLoop {
+  int32_t it;     // step number (slot rotation)
+  int32_t in;     // frontier queue read by this step
+  int32_t cur;    // window start
+  int32_t g, gh;  // low / high pile generations
+  int32_t hz;     // horizon
+  int32_t k;      // horizon width in buckets
+  int32_t phase;  // 0: normal, 1: after a lo-min, 2: after a hi-min
+  int32_t relax, adv;
+};
+constexpr int kBqLoopInts = 10;
+static_assert(sizeof(BqLoop) == kBqLoopInts * sizeof(int32_t), "BqLoop is published as ints");
+
+struct BqStep {
+  int32_t kind, work, m;
+};
+
+// The next step (pure: every CTA computes the same one).
+__device__ __forceinline__ BqStep bq_decide(const BqLoop &s, const int32_t *ctl, int32_t delta) {
+  const volatile int32_t *c = ctl;
+  const int32_t prev = (s.it + 2) % 3;
+  if (s.phase == 1) {
+    const int32_t m = c[BQ_MIN + prev];
+    if (m != INT_MAX) {
+      const bool cross = bq_clamp((int64_t)m + delta) > s.hz;  // the window reaches the high pile
+      return BqStep{BQ_LOSPLIT, c[BQ_LO + (s.g & 1)] + (cross ? c[BQ_HI + (s.gh & 1)] : 0), m};
     }
-    clk.tick(a.stop);
-    if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
-    in ^= 1;
+    const int32_t nh = c[BQ_HI + (s.gh & 1)];
+    return nh > 0 ? BqStep{BQ_HIMIN, nh, 0} : BqStep{BQ_DONE, 0, 0};
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    a.stats[0] = (int32_t)relax;
-    a.stats[1] = (int32_t)adv;
+  if (s.phase == 2) {
+    const int32_t m = c[BQ_MIN + prev];
+    return m != INT_MAX ? BqStep{BQ_HISPLIT, c[BQ_HI + (s.gh & 1)], m} : BqStep{BQ_DONE, 0, 0};
+  }
+  const int32_t n = c[BQ_NEAR + prev];
+  if (n > 0) return BqStep{BQ_RELAX, n, 0};
+  const int32_t nl = c[BQ_LO + (s.g & 1)];
+  if (nl > 0) return BqStep{BQ_LOMIN, nl, 0};
+  const int32_t nh = c[BQ_HI + (s.gh & 1)];
+  return nh > 0 ? BqStep{BQ_HIMIN, nh, 0} : BqStep{BQ_DONE, 0, 0};
+}
+
+// One step, CTA `rank` of `nparts` taking its share.
+template <int LB>
+__device__ __forceinline__ void bq_step(BqLoop &s, const BqArgs &a, const BqStep &st, int32_t rank,
+                                        int32_t nparts, int4 *smem, int32_t *red) {
+  int32_t *ctl = a.b.ctl;
+  const bool lead = rank == 0 && threadIdx.x == 0;
+  if (lead) {
+    ctl[BQ_NEAR + (s.it + 1) % 3] = 0;
+    ctl[BQ_MIN + (s.it + 1) % 3] = INT_MAX;
+  }
+  const int32_t U = bq_clamp((int64_t)s.cur + a.delta);  // cutoff of the current window
+  int32_t *qin = s.in ? a.q1 : a.q0, *qout = s.in ? a.q0 : a.q1;
+  DOut front{};
+  front.mode = OUT_SPARSE;
+  front.q = qout;
+  front.cnt = ctl + BQ_NEAR + s.it % 3;
+  front.cap = a.qcap;
+  front.err = a.err;
+  const int32_t lo_next = (s.g + 1) & 1;
+  switch (st.kind) {
+    case BQ_RELAX: {
+      const DFar far{a.b.stamp, a.b.lo[s.g & 1], ctl + BQ_LO + (s.g & 1), a.b.hi[s.gh & 1],
+                     ctl + BQ_HI + (s.gh & 1), bq_lo_tag(s.g), bq_hi_tag(s.gh), s.hz, a.b.V, a.err};
+      const EdgeF<USssp, false> f{USssp{a.dist, U, far}, DIn{IN_ALL, nullptr, nullptr},
+                                  DIn{IN_ALL, nullptr, nullptr}, false};
+      const int32_t n = (int64_t)st.work > a.qcap ? (int32_t)a.qcap : st.work;  // past qcap only after a flagged overflow
+      run_lb<LB>(a.g, Enum{qin, nullptr, n}, n, f, front, smem, rank, nparts);
+      s.in ^= 1;
+      s.relax++;
+      s.phase = 0;
+      break;
+    }
+    case BQ_LOMIN:
+      if (s.phase == 0) s.adv++;
+      if (lead) {
+        ctl[BQ_LO + lo_next] = 0;
+        ctl[BQ_HI + ((s.gh + 1) & 1)] = 0;
+        ctl[BQ_FILL + ((s.gh + 1) & 1)] = 0;
+      }
+      bq_pile_min(a.b.lo[s.g & 1], min(st.work, a.b.V), a.dist, U, ctl + BQ_MIN + s.it % 3, rank, nparts, red);
+      s.phase = 1;
+      break;
+    case BQ_LOSPLIT: {
+      const int32_t win = bq_clamp((int64_t)st.m + a.delta);
+      const int32_t n_lo = min(*(volatile int32_t *)(ctl + BQ_LO + (s.g & 1)), a.b.V);
+      if (win <= s.hz) {
+        const BqSplitOut o{a.b.stamp, a.b.lo[lo_next], ctl + BQ_LO + lo_next, bq_lo_tag(s.g + 1),
+                           nullptr, nullptr, 0, INT_MAX, nullptr, a.b.V, false};
+        bq_pile_split(a.b.lo[s.g & 1], n_lo, a.dist, U, win, front, o, a.err, rank, nparts);
+      } else {
+        // the window reaches past the horizon: split both piles under a new one
+        const int32_t hi_next = (s.gh + 1) & 1;
+        s.k = bq_adapt_width(s.k, *(volatile int32_t *)(ctl + BQ_FILL + (s.gh & 1)), a.fill_target);
+        const int32_t hz = bq_clamp((int64_t)st.m + (int64_t)s.k * a.delta);
+        BqSplitOut o{a.b.stamp, a.b.lo[lo_next], ctl + BQ_LO + lo_next, bq_lo_tag(s.g + 1),
+                     a.b.hi[hi_next], ctl + BQ_HI + hi_next, bq_hi_tag(s.gh + 1), hz, nullptr, a.b.V, true};
+        bq_pile_split(a.b.lo[s.g & 1], n_lo, a.dist, U, win, front, o, a.err, rank, nparts);
+        o.fill = ctl + BQ_FILL + hi_next;
+        bq_pile_split(a.b.hi[s.gh & 1], min(*(volatile int32_t *)(ctl + BQ_HI + (s.gh & 1)), a.b.V), a.dist, U,
+                      win, front, o, a.err, rank, nparts);
+        s.hz = hz;
+        s.gh++;
+      }
+      s.cur = st.m;
+      s.g++;
+      s.in ^= 1;
+      s.phase = 0;
+      break;
+    }
+    case BQ_HIMIN: {
+      if (s.phase == 0) s.adv++;
+      const int32_t hi_next = (s.gh + 1) & 1;
+      if (lead) {
+        ctl[BQ_LO + lo_next] = 0;
+        ctl[BQ_HI + hi_next] = 0;
+        ctl[BQ_FILL + hi_next] = 0;
+      }
+      bq_pile_min(a.b.hi[s.gh & 1], min(st.work, a.b.V), a.dist, U, ctl + BQ_MIN + s.it % 3, rank, nparts, red);
+      s.phase = 2;
+      break;
+    }
+    case BQ_HISPLIT: {
+      const int32_t hi_next = (s.gh + 1) & 1;
+      s.k = bq_adapt_width(s.k, *(volatile int32_t *)(ctl + BQ_FILL + (s.gh & 1)), a.fill_target);
+      const int32_t hz = bq_clamp((int64_t)st.m + (int64_t)s.k * a.delta);
+      const BqSplitOut o{a.b.stamp, a.b.lo[lo_next], ctl + BQ_LO + lo_next, bq_lo_tag(s.g + 1),
+                         a.b.hi[hi_next], ctl + BQ_HI + hi_next, bq_hi_tag(s.gh + 1), hz,
+                         ctl + BQ_FILL + hi_next, a.b.V, false};
+      bq_pile_split(a.b.hi[s.gh & 1], min(st.work, a.b.V), a.dist, U, bq_clamp((int64_t)st.m + a.delta), front,
+                    o, a.err, rank, nparts);
+      s.cur = st.m;
+      s.hz = hz;
+      s.g++;
+      s.gh++;
+      s.in ^= 1;
+      s.phase = 0;
+      break;
+    }
+    default:
+      break;
+  }
+  s.it++;
+}
+
+// Loop state of CTA 0 for the other CTAs (read after the next barrier).
+__device__ __forceinline__ void bq_publish(const BqLoop &s, int32_t *ctl) {
+  if (threadIdx.x == 0) {
+    const int32_t *p = reinterpret_cast<const int32_t *>(&s);
+    for (int i = 0; i < kBqLoopInts; ++i) ctl[BQ_PUB + i] = p[i];
   }
 }
 
-template <class K>
-static gg_status coop_launch(gg_graph *g, K kernel, int cta, size_t smem, FusedArgs &a) {
+// CTA 0 alone: steps while they stay small (see above), then publishes the
+// loop state.  The whole CTA calls it.
+template <int LB>
+__device__ __forceinline__ void bq_solo(BqLoop &s, const BqArgs &a, BqStep st, int4 *smem, int32_t *red,
+                                        int32_t *flag) {
+  uint64_t t0 = 0;
+  if (threadIdx.x == 0) t0 = globaltimer_ns();
+  for (;;) {
+    bq_step<LB>(s, a, st, 0, 1, smem, red);
+    __syncthreads();
+    if (threadIdx.x == 0)
+      *flag = (*(volatile int32_t *)a.err & DEV_ERR_OVERFLOW) != 0 || globaltimer_ns() - t0 > kSoloSliceNs;
+    __syncthreads();
+    const bool quit = *flag != 0;
+    __syncthreads();
+    if (quit) break;
+    st = bq_decide(s, a.b.ctl, a.delta);
+    if (st.kind == BQ_DONE || st.work > a.solo_max) break;
+  }
+  bq_publish(s, a.b.ctl);
+}
+
+template <int LB>
+__global__ void __launch_bounds__(1024) k_sssp_bq(BqArgs a) {
+  extern __shared__ int4 smem[];
+  __shared__ int32_t red[33];
+  BqLoop s{1, 0, 0, 0, 0, bq_clamp((int64_t)a.width0 * a.delta), a.width0, 0, 0, 0};
+  int32_t *stop = a.b.ctl + BQ_STOP;
+  LoopClock clk;
+  clk.start(a.loop_limit_ns);
+  for (;;) {
+    if (stopped(stop, a.err) || (*(volatile int32_t *)a.err & (DEV_ERR_OVERFLOW | DEV_ERR_TIMEOUT))) break;
+    const BqStep st = bq_decide(s, a.b.ctl, a.delta);
+    if (st.kind == BQ_DONE) {
+      if (s.phase == 0) s.adv++;  // the reference's last advance finds no priority left
+      break;
+    }
+    if (st.work <= a.solo_max) {
+      // CTA 0 starts changing the control words only once every other CTA
+      // has taken its decision from them and arrived at the barrier.
+      if (blockIdx.x == 0) {
+        if (grid_wait_others(a.bar, gridDim.x, a.err, a.timeout_ns))
+          bq_solo<LB>(s, a, st, smem, red, red + 32);
+        else
+          bq_publish(s, a.b.ctl);
+      }
+      clk.tick(stop);
+      if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
+      const volatile int32_t *pub = a.b.ctl + BQ_PUB;
+      int32_t *p = reinterpret_cast<int32_t *>(&s);
+      for (int i = 0; i < kBqLoopInts; ++i) p[i] = pub[i];
+      continue;
+    }
+    bq_step<LB>(s, a, st, blockIdx.x, gridDim.x, smem, red);
+    clk.tick(stop);
+    if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.b.ctl[BQ_STATS] = s.relax;
+    a.b.ctl[BQ_STATS + 1] = s.adv;
+  }
+}
+
+// Control words at the start of a run: n0 sources on the first frontier, no
+// minima, empty piles, no refill yet.
+__global__ void k_bq_init(int32_t *ctl, int32_t n0) {
+  const int32_t i = threadIdx.x;
+  if (i >= BQ_CTL_INTS) return;
+  int32_t v = 0;
+  if (i == BQ_NEAR) v = n0;
+  if (i >= BQ_MIN && i < BQ_MIN + 3) v = INT_MAX;
+  if (i == BQ_FILL) v = -1;
+  ctl[i] = v;
+}
+
+gg_status bq_start(const BqBuffers &b, int32_t n0, cudaStream_t st) {
+  GG_CUDA(cudaMemsetAsync(b.stamp, 0, sizeof(int32_t) * (size_t)std::max(b.V, 1), st));
+  note_launch();
+  k_bq_init<<<1, BQ_CTL_INTS, 0, st>>>(b.ctl, n0);
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+template <class K, class A>
+static gg_status coop_launch(gg_graph *g, K kernel, int cta, size_t smem, A &a) {
   int per_sm = 0;
   if (smem > 48 * 1024)
     GG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -281,22 +485,55 @@ gg_status fused_bfs(gg_graph *g, const gg_schedule *s, int32_t n0, const VData &
   return GG_OK;
 }
 
+// Largest step the SSSP loop runs on one CTA (GG_BQ_SOLO_MAX overrides; 0
+// turns the one-CTA mode off).
+static int32_t bq_solo_max(int cta) {
+  static const long env = [] {
+    const char *e = getenv("GG_BQ_SOLO_MAX");
+    return e ? atol(e) : -1L;
+  }();
+  return env >= 0 ? (int32_t)env : 2 * cta;
+}
+
+static BqArgs bq_args(gg_graph *g, gg_frontier *f, const BqBuffers &b, int32_t *dist, int32_t delta, int cta) {
+  BqArgs a{};
+  a.g = g->csr.view();
+  a.g.nbuckets = 0;
+  a.q0 = f->q_in;
+  a.q1 = f->q_out;
+  a.qcap = f->cap;
+  a.dist = dist;
+  a.b = b;
+  a.bar = g->d_bar;
+  a.err = g->d_err;
+  a.timeout_ns = barrier_timeout_ns();
+  a.loop_limit_ns = loop_timeout_ns();
+  a.delta = delta;
+  a.solo_max = bq_solo_max(cta);
+  a.fill_target = 4096;
+  a.width0 = 16;
+  return a;
+}
+
 gg_status fused_sssp(gg_graph *g, const gg_schedule *s, int32_t n0, int32_t delta, const VData &vd,
-                     gg_frontier *f, int32_t *iters, int64_t *advances, bool *ran) {
+                     gg_pq *pq, int32_t *iters, int64_t *advances, bool *ran) {
   *ran = false;
   if (!fused_supported(s)) return GG_OK;
-  GG_TRY(init_counts(g, n0));
-  FusedArgs a = make_args(g, f, vd);
-  a.delta = delta;
   const int cta = s->cta_size;
+  GG_TRY(bq_start(pq->bq, n0, g->stream));
+  BqArgs a = bq_args(g, pq->frontier, pq->bq, vd.dist, delta, cta);
   const size_t sm = lb_smem(s->load_balancing, cta);
   switch (s->load_balancing) {
-    case GG_LB_VERTEX_BASED: GG_TRY(coop_launch(g, k_sssp_fused<GG_LB_VERTEX_BASED>, cta, sm, a)); break;
-    case GG_LB_WM: GG_TRY(coop_launch(g, k_sssp_fused<GG_LB_WM>, cta, sm, a)); break;
-    case GG_LB_TWCE: GG_TRY(coop_launch(g, k_sssp_fused<GG_LB_TWCE>, cta, sm, a)); break;
-    default: GG_TRY(coop_launch(g, k_sssp_fused<GG_LB_CM>, cta, sm, a)); break;
+    case GG_LB_VERTEX_BASED: GG_TRY(coop_launch(g, k_sssp_bq<GG_LB_VERTEX_BASED>, cta, sm, a)); break;
+    case GG_LB_WM: GG_TRY(coop_launch(g, k_sssp_bq<GG_LB_WM>, cta, sm, a)); break;
+    case GG_LB_TWCE: GG_TRY(coop_launch(g, k_sssp_bq<GG_LB_TWCE>, cta, sm, a)); break;
+    default: GG_TRY(coop_launch(g, k_sssp_bq<GG_LB_CM>, cta, sm, a)); break;
   }
-  GG_TRY(read_stats(g, iters, advances));
+  GG_CUDA(cudaMemcpyAsync(g->h_pinned + 50, pq->bq.ctl + BQ_STATS, sizeof(int32_t) * 2, cudaMemcpyDeviceToHost,
+                          g->stream));
+  GG_CUDA(cudaStreamSynchronize(g->stream));
+  *iters = g->h_pinned[50];
+  *advances = g->h_pinned[51];
   *ran = true;
   return GG_OK;
 }
@@ -341,9 +578,11 @@ __global__ void k_multi_seed(VData vd, int32_t sssp, const int32_t *__restrict__
 }
 
 gg_status fused_multi_enqueue(gg_graph *g, cudaStream_t st, bool sssp, const int32_t *dsrc, int32_t n,
-                              int32_t delta, int32_t *parent, int32_t *out) {
+                              int32_t delta, int32_t *parent, int32_t *out, const BqBuffers *bq,
+                              const int32_t **stats) {
   gg_frontier *f = g->app_frontier;
   if (!f) return set_error(GG_ERR_STATE, "multi-source run: the graph's frontier is not created");
+  if (sssp && !bq) return set_error(GG_ERR_STATE, "multi-source SSSP needs its bucket-queue buffers");
   VData vd{};
   if (sssp) {
     vd.dist = out;
@@ -356,7 +595,7 @@ gg_status fused_multi_enqueue(gg_graph *g, cudaStream_t st, bool sssp, const int
   a.delta = delta;
   const int cta = 512;
   const size_t smem = twce_smem_bytes(cta);
-  const void *kernel = sssp ? (const void *)k_sssp_fused<GG_LB_TWCE> : (const void *)k_bfs_fused<GG_LB_TWCE>;
+  const void *kernel = sssp ? (const void *)k_sssp_bq<GG_LB_TWCE> : (const void *)k_bfs_fused<GG_LB_TWCE>;
   int per_sm = 0;
   GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, cta, smem));
   if (per_sm < 1) return set_error(GG_ERR_UNSUPPORTED, "fused kernel does not fit on an SM");
@@ -366,9 +605,19 @@ gg_status fused_multi_enqueue(gg_graph *g, cudaStream_t st, bool sssp, const int
   k_multi_seed<<<std::max(1, std::min(ceil_div(n, 256), g->sm_count)), 256, 0, st>>>(
       vd, sssp, dsrc, n, a.q0, a.cnt3, a.stats, a.gmin2, a.stop);
   GG_CUDA(cudaMemsetAsync(g->d_bar, 0, sizeof(uint32_t) * 2, st));
-  void *args[] = {&a};
-  note_launch();
-  GG_CUDA(cudaLaunchCooperativeKernel(kernel, per_sm * g->sm_count, cta, args, smem, st));
+  if (sssp) {
+    GG_TRY(bq_start(*bq, n, st));
+    BqArgs b = bq_args(g, f, *bq, out, delta, cta);
+    void *args[] = {&b};
+    note_launch();
+    GG_CUDA(cudaLaunchCooperativeKernel(kernel, per_sm * g->sm_count, cta, args, smem, st));
+    if (stats) *stats = bq->ctl + BQ_STATS;
+  } else {
+    void *args[] = {&a};
+    note_launch();
+    GG_CUDA(cudaLaunchCooperativeKernel(kernel, per_sm * g->sm_count, cta, args, smem, st));
+    if (stats) *stats = a.stats;
+  }
   return GG_OK;
 }
 

@@ -6,6 +6,7 @@
 //  - get_blocked_graph (graph.h:105-163, a host bucketing by dst/block_size
 //    that also frees the source arrays) is a GPU bucketing into a separate copy.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -201,6 +202,18 @@ std::mutex g_pool_mu;
 cudaMemPool_t g_pool[kMaxDevices] = {};
 }  // namespace
 
+// GG_DEVICE_POOL_LIMIT_BYTES caps what the pool hands out (allocations beyond
+// it fail as out of memory): a way to run the engine inside a fixed memory
+// budget, and to exercise the GG_ERR_OOM path without exhausting a GPU.
+static uint64_t pool_limit_bytes() {
+  static const uint64_t lim = [] {
+    const char *e = getenv("GG_DEVICE_POOL_LIMIT_BYTES");
+    const unsigned long long v = e ? strtoull(e, nullptr, 10) : 0ull;
+    return v ? (uint64_t)v : UINT64_MAX;
+  }();
+  return lim;
+}
+
 cudaError_t dev_alloc(void **p, size_t bytes, cudaStream_t st) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -222,6 +235,13 @@ cudaError_t dev_alloc(void **p, size_t bytes, cudaStream_t st) {
       if (e != cudaSuccess) return e;
     }
     pool = g_pool[dev];
+  }
+  const uint64_t limit = pool_limit_bytes();
+  if (limit != UINT64_MAX) {
+    uint64_t used = 0;
+    e = cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used);
+    if (e != cudaSuccess) return e;
+    if (used + bytes > limit) return cudaErrorMemoryAllocation;
   }
   return cudaMallocFromPoolAsync(p, bytes, pool, st);
 }
@@ -389,13 +409,10 @@ using namespace gg;
 
 extern "C" {
 
-gg_status gg_graph_create(const int32_t *offsets, const int32_t *dst, const int32_t *weights,
-                          int32_t V, int64_t E, uint32_t flags, gg_graph **out) {
-  GG_CHECK_ARG(out && offsets, "offsets/out is NULL");
-  GG_CHECK_ARG(V > 0, "graph needs at least one vertex");
-  GG_CHECK_ARG(E >= 0 && E <= INT32_MAX, "edge count outside the int32 CSR layout");
-  GG_CHECK_ARG(E == 0 || dst, "dst is NULL");
-  auto g = std::make_unique<gg_graph>();
+// Everything gg_graph_create sets up; on failure the caller releases what was
+// made (gg_graph_destroy takes a partly built graph).
+static gg_status graph_init(gg_graph *g, const int32_t *offsets, const int32_t *dst, const int32_t *weights,
+                            int32_t V, int64_t E, uint32_t flags) {
   GG_CUDA(cudaGetDevice(&g->device));
   GG_CUDA(cudaDeviceGetAttribute(&g->sm_count, cudaDevAttrMultiProcessorCount, g->device));
   GG_CUDA(cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking));
@@ -432,7 +449,23 @@ gg_status gg_graph_create(const int32_t *offsets, const int32_t *dst, const int3
   GG_CUDA(cudaEventCreate(&g->ev2));
   GG_CUDA(cudaEventCreate(&g->ev3));
   GG_CUDA(cudaStreamSynchronize(st));  // the COO source column is built on first use (ensure_coo)
-  *out = g.release();
+  return GG_OK;
+}
+
+gg_status gg_graph_create(const int32_t *offsets, const int32_t *dst, const int32_t *weights,
+                          int32_t V, int64_t E, uint32_t flags, gg_graph **out) {
+  GG_CHECK_ARG(out && offsets, "offsets/out is NULL");
+  GG_CHECK_ARG(V > 0, "graph needs at least one vertex");
+  GG_CHECK_ARG(E >= 0 && E <= INT32_MAX, "edge count outside the int32 CSR layout");
+  GG_CHECK_ARG(E == 0 || dst, "dst is NULL");
+  auto *g = new (std::nothrow) gg_graph();
+  if (!g) return set_error(GG_ERR_OOM, "graph handle allocation failed");
+  const gg_status st = graph_init(g, offsets, dst, weights, V, E, flags);
+  if (st != GG_OK) {
+    gg_graph_destroy(g);  // the pool takes back what was allocated
+    return st;
+  }
+  *out = g;
   return GG_OK;
 }
 

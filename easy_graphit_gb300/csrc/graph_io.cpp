@@ -316,9 +316,108 @@ gg_status load_text(const std::string &path, bool symmetrize, gg_host_graph **ou
   return build_csr(max_id + 1, el, symmetrize || force_sym, out);
 }
 
+// GAPBS serialized graphs (infra_gapbs/reader.h:322-369, writer.h:39-70):
+//   [bool directed][i64 num_edges][i64 num_nodes][i64 offsets[V+1]][neighbours[E]]
+//   and, when directed, the in-lists in the same two arrays again.
+// A .sg neighbour is an int32 id, a .wsg one an {int32 id, int32 weight} pair.
+// The out-lists are taken as they are stored (GAPBS writes squished graphs);
+// the in-lists are skipped.
+gg_status load_sg(const std::string &path, bool weighted, gg_host_graph **out) {
+  FILE *f = fopen(path.c_str(), "rb");
+  if (!f) return gg::set_error(GG_ERR_IO, "cannot open %s: %s", path.c_str(), strerror(errno));
+  unsigned char directed = 0;
+  int64_t E = 0, V = 0;
+  const bool hdr = fread(&directed, 1, 1, f) == 1 && fread(&E, 8, 1, f) == 1 && fread(&V, 8, 1, f) == 1;
+  fseek(f, 0, SEEK_END);
+  const long long size = ftell(f);
+  const long long nb = weighted ? 8 : 4;
+  const long long one = 8LL * (V + 1) + nb * E;
+  if (!hdr || directed > 1 || V <= 0 || V > INT32_MAX - 1 || E < 0 || E > INT32_MAX ||
+      size != 17 + one * (directed ? 2 : 1)) {
+    fclose(f);
+    return gg::set_error(GG_ERR_IO, "%s: header (V=%lld, E=%lld) does not match the file size %lld",
+                         path.c_str(), (long long)V, (long long)E, size);
+  }
+  fseek(f, 17, SEEK_SET);
+  std::vector<int64_t> off(V + 1);
+  std::vector<int32_t> nbr((size_t)E * (weighted ? 2 : 1));
+  const bool ok = fread(off.data(), 8, V + 1, f) == (size_t)(V + 1) &&
+                  fread(nbr.data(), nb, E, f) == (size_t)E;
+  fclose(f);
+  if (!ok) return gg::set_error(GG_ERR_IO, "%s: short read", path.c_str());
+  bool valid = off[0] == 0 && off[V] == E;
+  for (int64_t v = 0; valid && v < V; ++v) valid = off[v] <= off[v + 1];
+  auto *g = new (std::nothrow) gg_host_graph();
+  if (!g) return gg::set_error(GG_ERR_OOM, "host graph allocation failed");
+  g->V = (int32_t)V;
+  g->E = E;
+  g->offsets.resize(V + 1);
+  g->dst.resize(E);
+  g->w.resize(E);
+  for (int64_t v = 0; valid && v <= V; ++v) g->offsets[v] = (int32_t)off[v];
+  for (int64_t k = 0; valid && k < E; ++k) {
+    const int32_t d = weighted ? nbr[2 * k] : nbr[k];
+    valid = d >= 0 && d < V;
+    g->dst[k] = d;
+    g->w[k] = weighted ? nbr[2 * k + 1] : 1;
+  }
+  if (!valid) {
+    delete g;
+    return gg::set_error(GG_ERR_IO, "%s: corrupt offsets or neighbour ids", path.c_str());
+  }
+  *out = g;
+  return GG_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+gg_status gg_host_graph_save_sg(const gg_host_graph *g, const char *path, int32_t directed) {
+  GG_CHECK_ARG(g && path, "bad arguments");
+  const std::string p(path);
+  const bool weighted = ends_with(p, ".wsg");
+  GG_CHECK_ARG(weighted || ends_with(p, ".sg"), "a serialized graph file ends in .sg or .wsg");
+  const int64_t V = g->V, E = g->E;
+  std::vector<int64_t> off(V + 1);
+  auto lists = [&](const int32_t *o, const int32_t *d, const int32_t *w, std::vector<int32_t> &buf) {
+    for (int64_t v = 0; v <= V; ++v) off[v] = o[v];
+    buf.resize((size_t)E * (weighted ? 2 : 1));
+    for (int64_t k = 0; k < E; ++k) {
+      if (weighted) {
+        buf[2 * k] = d[k];
+        buf[2 * k + 1] = w[k];
+      } else {
+        buf[k] = d[k];
+      }
+    }
+  };
+  FILE *f = fopen(path, "wb");
+  if (!f) return gg::set_error(GG_ERR_IO, "cannot create %s: %s", path, strerror(errno));
+  const unsigned char dir = directed ? 1 : 0;
+  std::vector<int32_t> buf;
+  lists(g->offsets.data(), g->dst.data(), g->w.data(), buf);
+  const size_t nb = weighted ? 8 : 4;
+  bool ok = fwrite(&dir, 1, 1, f) == 1 && fwrite(&E, 8, 1, f) == 1 && fwrite(&V, 8, 1, f) == 1 &&
+            fwrite(off.data(), 8, V + 1, f) == (size_t)(V + 1) && fwrite(buf.data(), nb, E, f) == (size_t)E;
+  if (ok && directed) {
+    // in-lists: sources of each vertex's in-edges in ascending order, with weights
+    std::vector<int32_t> io(V + 1, 0), isrc(E), iw(E);
+    for (int64_t k = 0; k < E; ++k) io[g->dst[k] + 1]++;
+    for (int64_t v = 0; v < V; ++v) io[v + 1] += io[v];
+    std::vector<int32_t> pos(io.begin(), io.end() - 1);
+    for (int64_t u = 0; u < V; ++u)
+      for (int64_t k = g->offsets[u]; k < g->offsets[u + 1]; ++k) {
+        isrc[pos[g->dst[k]]] = (int32_t)u;
+        iw[pos[g->dst[k]]++] = g->w[k];
+      }
+    lists(io.data(), isrc.data(), iw.data(), buf);
+    ok = fwrite(off.data(), 8, V + 1, f) == (size_t)(V + 1) && fwrite(buf.data(), nb, E, f) == (size_t)E;
+  }
+  ok = (fclose(f) == 0) && ok;
+  if (!ok) return gg::set_error(GG_ERR_IO, "short write to %s", path);
+  return GG_OK;
+}
 
 gg_status gg_host_graph_rmat(int32_t scale, int32_t degree, float a, float b,
                              float c, int64_t seed, int32_t symmetrize,
@@ -424,6 +523,7 @@ gg_status gg_host_graph_load(const char *path, int32_t symmetrize, gg_host_graph
   GG_CHECK_ARG(path && out, "bad arguments");
   const std::string p(path);
   if (ends_with(p, ".graphit_bin")) return load_bin(p, out);
+  if (ends_with(p, ".sg") || ends_with(p, ".wsg")) return load_sg(p, ends_with(p, ".wsg"), out);
   return load_text(p, symmetrize != 0, out);
 }
 

@@ -28,10 +28,25 @@ __device__ __forceinline__ void do_edge(const DGraph &g, const F &f, const DOut 
   if (t >= 0) out.push(t);
 }
 
+template <class F, class = void>
+struct lb_batch {
+  static constexpr bool value = false;
+};
+template <class F>
+struct lb_batch<F, decltype(void(F::kBatch))> {
+  static constexpr bool value = F::kBatch;
+};
+
 // Edges [b, e) of source s processed by `width` cooperating threads (rank r).
+// A functor with a batched range relax (push, no per-edge source test beyond
+// the first) takes the whole range at once.
 template <class F>
 __device__ __forceinline__ void do_range(const DGraph &g, const F &f, const DOut &out, int32_t s,
                                          int32_t b, int32_t e, int32_t r, int32_t width) {
+  if constexpr (lb_batch<F>::value) {
+    if (b + r < e && f.src_ok(s)) f.relax_range(g, out, s, b, e, r, width);
+    return;
+  }
   for (int32_t k = b + r; k < e; k += width) {
     if (!f.src_ok(s)) break;
     do_edge(g, f, out, s, k);

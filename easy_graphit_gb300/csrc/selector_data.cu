@@ -244,7 +244,12 @@ extern "C" gg_status gg_selector_collect(gg_graph *g, int32_t app, int32_t src, 
         return edgeset_apply_impl(g, &sc, GG_UDF_SSSP_RELAX, GG_FILTER_NONE, f, f, true, vd, cutoff, false);
       };
       GG_TRY(time_candidates(g, f, snap, base, true, apply, times + (size_t)*nrows * kCandidates));
-      GG_TRY(apply(base));
+      // candidates are timed without parking far improvements (the same for
+      // all of them, and nothing to restore); the step that moves the run on
+      // parks them so the queue's next advance finds them
+      VData vf = vd;
+      vf.far = pq_far(pq);
+      GG_TRY(edgeset_apply_impl(g, &base, GG_UDF_SSSP_RELAX, GG_FILTER_NONE, f, f, true, vf, cutoff, false));
       rt.visited_v = std::min<double>(V, rt.visited_v + fs.n);
       rt.visited_e = std::min<double>(g->csr.E, rt.visited_e + fs.sum_deg);
       rt.iteration++;

@@ -29,17 +29,61 @@ struct UBfs {
 };
 
 // sssp.cpp:24-27 + PriorityQueue::updatePriorityMin (graphit_types.h:426-430):
-// writeMin(&SP[dst], SP[src]+w) && new < prio_cutoff  => enqueue dst.
+// writeMin(&SP[dst], SP[src]+w) && new < prio_cutoff  => enqueue dst.  An
+// improvement at or above the cutoff parks dst on the queue's far piles
+// (when the queue keeps them), which is how the next bucket is found without
+// scanning every vertex.
 struct USssp {
   static constexpr bool kWeight = true;
+  static constexpr bool kBatch = true;  // push relax over a range: relax_range
+  static constexpr int kEdgesInFlight = 4;
   int32_t *dist;
   int32_t cutoff;
+  DFar far;
   __device__ __forceinline__ bool filter(int32_t) const { return true; }
   __device__ __forceinline__ bool apply(int32_t s, int32_t d, int32_t w) const {
     const int32_t ds = vload(dist + s);
     if (ds == INT_MAX) return false;
     const int32_t np = ds + w;
-    return write_min(dist + d, np) && np < cutoff;
+    if (!write_min(dist + d, np)) return false;
+    if (np < cutoff) return true;
+    if (far.stamp) far.park(d, np);
+    return false;
+  }
+  // Edges k = b + r, b + r + width, ... of source s, kEdgesInFlight at a time:
+  // their targets and weights, then the targets' distances, then the
+  // atomicMins of the improving ones are each issued together, so one thread
+  // keeps that many edges in flight instead of one (a hub's list on a thread
+  // of VERTEX_BASED is otherwise a chain of dependent round trips).  Same
+  // outcome as apply() per edge: an improvement below the cutoff queues the
+  // target, one above it parks it.
+  template <class G, class Out>
+  __device__ __forceinline__ void relax_range(const G &g, const Out &out, int32_t s, int32_t b, int32_t e,
+                                              int32_t r, int32_t width) const {
+    const int32_t ds = vload(dist + s);
+    if (ds == INT_MAX) return;
+    constexpr int B = kEdgesInFlight;
+    for (int32_t k0 = b + r; k0 < e; k0 += B * width) {
+      int32_t d[B], np[B], prev[B];
+#pragma unroll
+      for (int j = 0; j < B; ++j) {
+        const int32_t k = k0 + j * width;
+        d[j] = k < e ? __ldg(g.dst + k) : -1;
+        np[j] = k < e ? ds + __ldg(g.w + k) : INT_MAX;
+      }
+#pragma unroll
+      for (int j = 0; j < B; ++j) prev[j] = d[j] >= 0 ? __ldcg(dist + d[j]) : INT_MIN;
+#pragma unroll
+      for (int j = 0; j < B; ++j) prev[j] = np[j] < prev[j] ? atomicMin(dist + d[j], np[j]) : INT_MIN;
+#pragma unroll
+      for (int j = 0; j < B; ++j) {
+        if (prev[j] <= np[j]) continue;
+        if (np[j] < cutoff)
+          out.push(d[j]);
+        else if (far.stamp)
+          far.park(d[j], np[j]);
+      }
+    }
   }
 };
 
@@ -108,9 +152,21 @@ struct UBcB {
 // PULL: enumerate the reverse frontier on the transposed graph, src filter =
 // to() (checked before every edge: the early exit), dst filter = membership in
 // the from-frontier, and the UDF called with swapped arguments.
+template <class U, class = void>
+struct batch_of {
+  static constexpr bool value = false;
+};
+template <class U>
+struct batch_of<U, decltype(void(U::kBatch))> {
+  static constexpr bool value = U::kBatch;
+};
+
 template <class U, bool PULL>
 struct EdgeF {
   static constexpr bool kWeight = U::kWeight;
+  // push direction with a UDF that has a batched range relax (its to() filter
+  // passes every vertex, so the range needs no per-edge destination test)
+  static constexpr bool kBatch = !PULL && batch_of<U>::value;
   U u;
   DIn in_src, in_dst;
   bool filt;
@@ -125,6 +181,12 @@ struct EdgeF {
   __device__ __forceinline__ int32_t apply(int32_t s, int32_t d, int32_t w) const {
     if (PULL) return u.apply(d, s, w) ? s : -1;
     return u.apply(s, d, w) ? d : -1;
+  }
+  // Only used when kBatch; the source filter (in_src) is checked by the caller.
+  template <class G, class Out>
+  __device__ __forceinline__ void relax_range(const G &g, const Out &out, int32_t s, int32_t b, int32_t e,
+                                              int32_t r, int32_t width) const {
+    if constexpr (kBatch) u.relax_range(g, out, s, b, e, r, width);
   }
 };
 

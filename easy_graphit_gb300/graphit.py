@@ -124,19 +124,39 @@ class SimpleGPUSchedule:
 
 class HybridGPUSchedule:
     """graphit::HybridGPUSchedule (schedule.h:122-139): s1 when
-    |frontier| <= threshold * V, else s2 (operators.cpp:526)."""
+    |frontier| <= threshold * V, else s2 (operators.cpp:526).
+
+    configThreshold(t) fixes the threshold; bindThreshold(ref) binds it to a
+    value the caller keeps changing (schedule.cpp:9-12 binds a dyn_var<float>):
+    a one-element list or array, a ctypes float, or a callable, read every
+    time the schedule decides."""
 
     def __init__(self, s1: SimpleGPUSchedule, s2: SimpleGPUSchedule):
         self.s1, self.s2 = s1, s2
-        self.threshold = 0.0
+        self._static = 0.0
+        self._bound = None
 
     def configThreshold(self, t: float):
-        self.threshold = float(t)
+        self._static = float(t)
+        self._bound = None
         return self
 
-    def bindThreshold(self, t: float):  # the runtime-bound threshold of schedule.cpp:9-12
-        self.threshold = float(t)
+    def bindThreshold(self, ref):
+        if isinstance(ref, (int, float)):  # a plain number cannot be rebound later: same as config
+            return self.configThreshold(ref)
+        self._bound = ref
         return self
+
+    @property
+    def threshold(self) -> float:
+        r = self._bound
+        if r is None:
+            return self._static
+        if callable(r):
+            return float(r())
+        if hasattr(r, "value"):
+            return float(r.value)
+        return float(r[0])
 
 
 D, LB, FC, PR_ = (SimpleGPUSchedule.direction_type, SimpleGPUSchedule.load_balancing_type,
@@ -257,6 +277,10 @@ class HostGraph:
     @classmethod
     def load(cls, path: str, symmetrize: bool = False) -> "HostGraph":
         return cls._make("gg_host_graph_load", str(path).encode(), int(symmetrize))
+
+    def save_sg(self, path: str, directed: bool = True) -> None:
+        """GAPBS serialized graph: .sg (ids) or .wsg (ids and weights)."""
+        call("gg_host_graph_save_sg", self._h, str(path).encode(), int(directed))
 
     def save_bin(self, path: str) -> None:
         call("gg_host_graph_save_bin", self._h, str(path).encode())
@@ -407,6 +431,14 @@ class VertexSubset:
         h = C.c_void_p()
         call("gg_frontier_create", g.handle, int(init_all), C.byref(h))
         self._h = h
+        self._owned = True
+
+    @classmethod
+    def _view(cls, g: GraphT, handle) -> "VertexSubset":
+        """A frontier owned by someone else (a priority queue's)."""
+        v = cls.__new__(cls)
+        v.g, v._h, v._owned = g, handle, False
+        return v
 
     @property
     def handle(self):
@@ -452,6 +484,191 @@ class VertexSubset:
             if getattr(self, "_h", None):
                 lib().gg_frontier_destroy(self._h)
                 self._h = None
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------ the operators
+class UDF(IntEnum):
+    """Edge UDFs of the five apps (gg.h GG_UDF_*)."""
+    BFS_PARENT = 0   # bfs.cpp:23-25
+    SSSP_RELAX = 1   # sssp.cpp:24-27
+    PR_ADD = 2       # pr.cpp:32-34
+    CC_HOOK = 3      # cc.cpp:23-36
+    BC_FORWARD = 4   # bc.cpp:34-36
+    BC_BACKWARD = 5  # bc.cpp:52-54
+
+
+class Filter(IntEnum):
+    """to() filters of the apps (gg.h GG_FILTER_*)."""
+    NONE = 0
+    PARENT_UNSET = 1  # bfs.cpp:27-29
+    UNVISITED = 2     # bc.cpp:38-40
+
+
+class VUDF(IntEnum):
+    """Vertex UDFs of the five apps (gg.h GG_VUDF_*)."""
+    BFS_RESET = 0
+    SSSP_RESET = 1
+    PR_RESET = 2
+    PR_CONTRIB = 3
+    PR_UPDATE = 4
+    CC_INIT = 5
+    CC_PJUMP = 6
+    BC_RESET = 7
+    BC_MARK_VISITED = 8
+    BC_MARK_UNVISITED = 9
+    BC_BACKWARD_VERTEX = 10
+    BC_FINAL = 11
+
+
+class VertexData:
+    """The VertexData<T> arrays the apps' UDFs touch (apps/*.cpp), as device
+    tensors (or raw device addresses) by member name: parent, depth, dist,
+    ids, updates, old_rank, new_rank, contrib, num_paths, dependences,
+    visited; plus the scalars level, src and damping."""
+
+    FIELDS = ("parent", "depth", "dist", "ids", "updates", "old_rank", "new_rank", "contrib",
+              "num_paths", "dependences", "visited")
+
+    def __init__(self, level: int = 0, src: int = -1, damping: float = 0.85, **arrays):
+        unknown = set(arrays) - set(self.FIELDS)
+        if unknown:
+            raise TypeError(f"unknown vertex data {sorted(unknown)}")
+        self.arrays = arrays
+        self.level, self.src, self.damping = level, src, damping
+
+    def to_c(self) -> L.gg_vertex_data:
+        d = L.gg_vertex_data()
+        for k, a in self.arrays.items():
+            setattr(d, k, a if isinstance(a, int) else (a.data_ptr() if a is not None else None))
+        d.level, d.src, d.damping = int(self.level), int(self.src), float(self.damping)
+        return d
+
+
+class edgeset_apply:
+    """graphit::edgeset_apply (operators.h:38-178):
+
+        edgeset_apply(s).from_(frontier).to(Filter.X).apply(g, udf, vd)
+        edgeset_apply(s).from_(frontier).to(...).apply_modified(g, out, vd, udf, allow_dupes)
+        edgeset_apply(s).from_(frontier).apply_priority(g, udf, pq, vd)
+
+    A HybridGPUSchedule picks s1 when |from| <= threshold * V, else s2, at each
+    call (operators.h:116-132).  `from_` is `from` in C++ (a Python keyword)."""
+
+    def __init__(self, schedule=None):
+        self.schedule = schedule if schedule is not None else SimpleGPUSchedule()
+        self.from_set: Optional[VertexSubset] = None
+        self.to_filter = Filter.NONE
+
+    def from_(self, f: "VertexSubset") -> "edgeset_apply":
+        self.from_set = f
+        return self
+
+    def to(self, filt) -> "edgeset_apply":
+        self.to_filter = Filter(filt)
+        return self
+
+    def _simple(self, g: "GraphT") -> SimpleGPUSchedule:
+        s = self.schedule
+        if isinstance(s, HybridGPUSchedule):
+            n = self.from_set.size() if self.from_set is not None else g.num_vertices
+            return s.s1 if n <= s.threshold * g.num_vertices else s.s2
+        if isinstance(s, LearnedGPUSchedule):
+            return s.fallback
+        return s
+
+    def _run(self, g, udf, vd: VertexData, out, allow_dupes: bool):
+        sc = self._simple(g).to_c()
+        cvd = vd.to_c()
+        call("gg_edgeset_apply", g.handle, C.byref(sc), int(udf), int(self.to_filter),
+             self.from_set.handle if self.from_set is not None else None,
+             out.handle if out is not None else None, int(bool(allow_dupes)), C.byref(cvd))
+
+    def apply(self, g: "GraphT", udf, vd: VertexData) -> None:
+        self._run(g, udf, vd, None, True)
+
+    def apply_modified(self, g: "GraphT", to: "VertexSubset", vd: VertexData, udf,
+                       allow_dupes: bool = True) -> None:
+        self._run(g, udf, vd, to, allow_dupes)
+
+    def apply_priority(self, g: "GraphT", udf, pq: "PriorityQueue", vd: VertexData | None = None) -> None:
+        if udf != UDF.SSSP_RELAX:
+            raise ValueError("apply_priority takes the SSSP relax UDF (updatePriorityMin)")
+        sc = self._simple(g).to_c()
+        cvd = (vd or VertexData()).to_c()
+        call("gg_edgeset_apply_priority", g.handle, C.byref(sc), pq.handle, C.byref(cvd))
+
+
+def vertexset_apply(target, vudf, vd: VertexData) -> None:
+    """vertexset_apply(set | graph, udf) (operators.cpp:10-65)."""
+    cvd = vd.to_c()
+    if isinstance(target, VertexSubset):
+        call("gg_vertexset_apply", target.g.handle, target.handle, int(vudf), C.byref(cvd))
+    else:
+        call("gg_vertexset_apply", target.handle, None, int(vudf), C.byref(cvd))
+
+
+class PriorityQueue:
+    """graphit_runtime::GPUPriorityQueue (gpu_priority_queue.h:21-247) with
+    pq.init(edges, SP, 0, delta, src) of sssp.cpp:39; `priorities` is the
+    device int32 array SP."""
+
+    def __init__(self, g: "GraphT", priorities, init_priority: int, delta: int, src: int):
+        self.g = g
+        self._prio = priorities
+        h = C.c_void_p()
+        call("gg_pq_create", g.handle, _ptr(priorities), init_priority, delta, src, C.byref(h))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def finished(self) -> bool:
+        f = C.c_int32()
+        call("gg_pq_finished", self._h, C.byref(f))
+        return bool(f.value)
+
+    def dequeue(self) -> "VertexSubset":
+        h = C.c_void_p()
+        call("gg_pq_dequeue", self._h, C.byref(h))
+        return VertexSubset._view(self.g, h)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().gg_pq_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class VertexFrontierList:
+    """graphit_runtime::VertexFrontierList (list.h:18-116), bc.cpp's level stack."""
+
+    def __init__(self, g: "GraphT"):
+        h = C.c_void_p()
+        call("gg_frontier_list_create", g.handle, C.byref(h))
+        self._h = h
+
+    def insert(self, f: "VertexSubset") -> None:
+        call("gg_frontier_list_insert", self._h, f.handle)
+
+    def retrieve(self, f: "VertexSubset") -> None:
+        call("gg_frontier_list_retrieve", self._h, f.handle)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().gg_frontier_list_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass
 

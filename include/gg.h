@@ -1,7 +1,7 @@
 /*
  * gg.h -- C ABI of libgg.so, the GB300 (sm_103a) edge-traversal engine that
  * stands in for GraphIt's GPU runtime (easy_graphit `runtime/gpu_intrinsics.h`
- * and `runtime/infra_gpu/*.h`) behind the GraphIt operator/schedule API
+ * and the `runtime/infra_gpu/` headers) behind the GraphIt operator/schedule API
  * (`include/graphit/operators.h`, `include/graphit/schedule.h`).
  *
  * Conventions (reference behaviour -> this ABI):
@@ -129,9 +129,16 @@ gg_status gg_host_graph_from_csr(int32_t num_vertices, int64_t num_edges,
                                  const int32_t *offsets, const int32_t *dst,
                                  const int32_t *weights, gg_host_graph **out);
 /* Loads .graphit_bin (graph.h:255-270), .el / .wel text edge lists
- * (infra_gapbs/reader.h:55-100) or .gr (DIMACS). */
+ * (infra_gapbs/reader.h:55-100), .gr (DIMACS), .mtx (MatrixMarket), or a GAPBS
+ * serialized graph .sg / .wsg (reader.h:322-369; the stored out-lists are
+ * taken as they are, symmetrize is ignored). */
 gg_status gg_host_graph_load(const char *path, int32_t symmetrize,
                              gg_host_graph **out);
+/* Writes a GAPBS serialized graph (writer.h:39-70): .sg (ids only) or .wsg
+ * (id, weight pairs) by the path's suffix; `directed` also stores the
+ * in-lists, as GAPBS does for a directed graph. */
+gg_status gg_host_graph_save_sg(const gg_host_graph *g, const char *path,
+                                int32_t directed);
 /* Writes the .graphit_bin cache format of graph.h:295-302:
  * [i32 V][i32 E][i32 src[E]][i32 dst[E]][i32 w[E]][i32 offsets[V+1]]. */
 gg_status gg_host_graph_save_bin(const gg_host_graph *g, const char *path);
@@ -202,7 +209,7 @@ gg_status gg_frontier_read(gg_frontier *f, int32_t *out, int32_t cap,
                            int32_t *n);
 
 /* ------------------------------------------------------------ vertex data
- * The VertexData<T> arrays the apps' UDFs touch (apps/*.cpp), as device
+ * The VertexData<T> arrays the apps' UDFs touch (the apps/ sources), as device
  * pointers.  Unused members may be NULL. */
 typedef struct gg_vertex_data {
   int32_t *parent;      /* bfs.cpp:19            (-1 = unvisited)        */

@@ -49,6 +49,12 @@ def lib() -> C.CDLL:
             "orc_cc_omp": (None, [i32, _P, _P, _P, i32]),
             "orc_bc": (None, [i32, _P, _P, i32, _P]),
             "orc_reached_edges": (i64, [i32, _P, _P]),
+            "orc_rmat": (_P, [i32, i32, f32, f32, f32, i64, i32, i32, i32]),
+            "orc_graph_vertices": (i32, [_P]),
+            "orc_graph_edges": (i64, [_P]),
+            "orc_graph_copy": (None, [_P, _P, _P, _P]),
+            "orc_graph_free": (None, [_P]),
+            "orc_pick_sources": (None, [i32, _P, i32, i64, _P]),
         }
         for k, (r, a) in sig.items():
             fn = getattr(L, k)
@@ -172,6 +178,35 @@ def transpose(off, dst):
     toff = np.zeros(V + 1, dtype=np.int64)
     np.add.at(toff, dst + 1, 1)
     return np.cumsum(toff).astype(np.int32), src[order].astype(np.int32)
+
+
+# ------------------------------------------------------------ input graphs
+K_RAND_SEED = 27491095  # GAPBS kRandSeed (runtime/infra_gapbs/util.h)
+
+
+def rmat(scale: int, degree: int = 16, symmetrize: bool = False, a: float = 0.57, b: float = 0.19,
+         c: float = 0.19, seed: int = K_RAND_SEED, wmin: int = 1, wmax: int = 255):
+    """(offsets, dst, weights) of the R-MAT CSR, built on the host cores by the
+    oracle's own restatement of GAPBS's generator and builder."""
+    L = lib()
+    h = L.orc_rmat(scale, degree, a, b, c, seed, int(symmetrize), wmin, wmax)
+    try:
+        V, E = L.orc_graph_vertices(h), L.orc_graph_edges(h)
+        off = np.empty(V + 1, dtype=np.int32)
+        dst = np.empty(E, dtype=np.int32)
+        w = np.empty(E, dtype=np.int32)
+        L.orc_graph_copy(h, _p(off), _p(dst), _p(w))
+    finally:
+        L.orc_graph_free(h)
+    return off, dst, w
+
+
+def pick_sources(off, n: int, seed: int = K_RAND_SEED):
+    """n sources as GAPBS's SourcePicker draws them."""
+    off = np.ascontiguousarray(off, dtype=np.int32)
+    out = np.empty(n, dtype=np.int32)
+    lib().orc_pick_sources(len(off) - 1, _p(off), n, seed, _p(out))
+    return out
 
 
 # ------------------------------------------------------ reference-built data

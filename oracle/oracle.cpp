@@ -18,7 +18,10 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <numeric>
 #include <queue>
+#include <random>
+#include <utility>
 #include <vector>
 
 #ifdef _OPENMP
@@ -529,6 +532,129 @@ int64_t orc_reached_edges(int32_t V, const int32_t *off, const int32_t *val) {
   for (int32_t v = 0; v < V; ++v)
     if (val[v] >= 0 && val[v] != INT_MAX) s += off[v + 1] - off[v];
   return s;
+}
+
+// ------------------------------------------------------------ input graphs
+// R-MAT input of the benchmarks, restated from GAPBS's generator and builder
+// (runtime/infra_gapbs/generator.h:45-55, 74-107, 125-139; builder.h:134-163,
+// 188-226), so the CPU legs build their graphs without the engine.  Edges come
+// in blocks of 2^18, each drawn by a std::mt19937 seeded with seed + block
+// index: `scale` float draws per edge pick a quadrant at every level.  Ids are
+// then permuted by one std::shuffle driven by std::mt19937(seed), and weights
+// U[wmin, wmax] are drawn per block with the same reseeding.  The CSR has V =
+// largest id + 1, neighbour lists sorted by (id, weight), repeated neighbours
+// merged into the first (lightest) copy, and self-loops dropped; symmetrize
+// adds every edge in both directions with its weight.  Pinned by the CSR
+// digests of tests/golden (made by the reference's own builder).
+struct OrcGraph {
+  int32_t V = 0;
+  std::vector<int32_t> off, dst, w;
+};
+
+void *orc_rmat(int32_t scale, int32_t degree, float a, float b, float c, int64_t seed,
+               int32_t symmetrize, int32_t wmin, int32_t wmax) {
+  const int64_t M = (int64_t(1) << scale) * degree;
+  const int64_t kEdgeBlock = int64_t(1) << 18;
+  const int64_t nblocks = (M + kEdgeBlock - 1) / kEdgeBlock;
+  std::vector<int32_t> eu(M), ev(M), ew(M);
+  const float ab = a + b, abc = a + b + c;
+#pragma omp parallel for schedule(static)
+  for (int64_t blk = 0; blk < nblocks; ++blk) {
+    std::mt19937 gen((std::mt19937::result_type)(seed + blk));
+    std::uniform_real_distribution<float> unit(0.0f, 1.0f);
+    const int64_t end = std::min(M, (blk + 1) * kEdgeBlock);
+    for (int64_t e = blk * kEdgeBlock; e < end; ++e) {
+      int32_t x = 0, y = 0;
+      for (int32_t lvl = 0; lvl < scale; ++lvl) {
+        const float r = unit(gen);
+        x = 2 * x + (r < ab ? 0 : 1);
+        y = 2 * y + (r < ab ? (r > a ? 1 : 0) : (r > abc ? 1 : 0));
+      }
+      eu[e] = x;
+      ev[e] = y;
+    }
+  }
+  std::vector<int32_t> relabel(size_t(1) << scale);
+  std::iota(relabel.begin(), relabel.end(), 0);
+  std::mt19937 perm_gen((std::mt19937::result_type)seed);
+  std::shuffle(relabel.begin(), relabel.end(), perm_gen);
+  int32_t top = 0;
+#pragma omp parallel for schedule(static) reduction(max : top)
+  for (int64_t blk = 0; blk < nblocks; ++blk) {
+    std::mt19937 gen((std::mt19937::result_type)(seed + blk));
+    std::uniform_int_distribution<int> draw(wmin, wmax);
+    const int64_t end = std::min(M, (blk + 1) * kEdgeBlock);
+    for (int64_t e = blk * kEdgeBlock; e < end; ++e) {
+      eu[e] = relabel[eu[e]];
+      ev[e] = relabel[ev[e]];
+      ew[e] = draw(gen);
+      top = std::max(top, std::max(eu[e], ev[e]));
+    }
+  }
+  auto *g = new OrcGraph();
+  const int32_t V = top + 1;
+  g->V = V;
+  // bucket (neighbour, weight) pairs by source, then sort and merge per vertex
+  std::vector<int64_t> start(V + 1, 0);
+  for (int64_t e = 0; e < M; ++e) {
+    start[eu[e] + 1]++;
+    if (symmetrize) start[ev[e] + 1]++;
+  }
+  for (int32_t v = 0; v < V; ++v) start[v + 1] += start[v];
+  std::vector<std::pair<int32_t, int32_t>> adj(start[V]);
+  {
+    std::vector<int64_t> fillp(start.begin(), start.end() - 1);
+    for (int64_t e = 0; e < M; ++e) {
+      adj[fillp[eu[e]]++] = {ev[e], ew[e]};
+      if (symmetrize) adj[fillp[ev[e]]++] = {eu[e], ew[e]};
+    }
+  }
+  std::vector<int32_t> keep(V, 0);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int32_t v = 0; v < V; ++v) {
+    auto *lo = adj.data() + start[v], *hi = adj.data() + start[v + 1];
+    std::sort(lo, hi);
+    int32_t k = 0;
+    for (auto *p = lo; p < hi; ++p) {
+      if (p->first == v) continue;
+      if (k > 0 && lo[k - 1].first == p->first) continue;
+      lo[k++] = *p;
+    }
+    keep[v] = k;
+  }
+  g->off.assign(V + 1, 0);
+  for (int32_t v = 0; v < V; ++v) g->off[v + 1] = g->off[v] + keep[v];
+  g->dst.resize(g->off[V]);
+  g->w.resize(g->off[V]);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int32_t v = 0; v < V; ++v)
+    for (int32_t k = 0; k < keep[v]; ++k) {
+      g->dst[g->off[v] + k] = adj[start[v] + k].first;
+      g->w[g->off[v] + k] = adj[start[v] + k].second;
+    }
+  return g;
+}
+
+int32_t orc_graph_vertices(const void *h) { return static_cast<const OrcGraph *>(h)->V; }
+int64_t orc_graph_edges(const void *h) { return (int64_t) static_cast<const OrcGraph *>(h)->dst.size(); }
+void orc_graph_copy(const void *h, int32_t *off, int32_t *dst, int32_t *w) {
+  const OrcGraph *g = static_cast<const OrcGraph *>(h);
+  std::copy(g->off.begin(), g->off.end(), off);
+  std::copy(g->dst.begin(), g->dst.end(), dst);
+  std::copy(g->w.begin(), g->w.end(), w);
+}
+void orc_graph_free(void *h) { delete static_cast<OrcGraph *>(h); }
+
+// GAPBS SourcePicker (runtime/infra_gapbs/benchmark.h:50-71): uniform ids
+// from one std::mt19937(seed), skipping vertices without out-edges.
+void orc_pick_sources(int32_t V, const int32_t *off, int32_t n, int64_t seed, int32_t *out) {
+  std::mt19937 gen((std::mt19937::result_type)seed);
+  std::uniform_int_distribution<int32_t> pick(0, V - 1);
+  for (int32_t i = 0; i < n; ++i) {
+    int32_t v = pick(gen);
+    while (off[v + 1] == off[v]) v = pick(gen);
+    out[i] = v;
+  }
 }
 
 }  // extern "C"

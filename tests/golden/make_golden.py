@@ -2,7 +2,7 @@
 
 Runs oracle/_ref/ref_gapbs -- easy_graphit's vendored GAPBS generator, builder
 and OrderedProcessingOperatorNoMerge SSSP (runtime/infra_gapbs/), compiled by
-`make -C oracle ref` where the reference tree lies -- and stores:
+`make -C oracle ref REF_DIR=<reference tree>` -- and stores:
   * graph/<name>/{sha256, V, E}: digests of the CSR the reference builds;
   * graph_small/{offsets,dst,w}: one full small CSR;
   * sssp/<name>/d<delta>: reference distances for a few sources;

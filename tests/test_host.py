@@ -126,6 +126,86 @@ def test_graphit_bin_truncated_and_corrupt(tmp_path):
     assert e.value.status == L.GG_ERR_IO
 
 
+def _gapbs_sg(path, directed, V, out_lists, in_lists=None, weighted=False):
+    """Writes GAPBS's serialized layout by hand (writer.h:39-70): [bool directed]
+    [i64 E][i64 V][i64 offsets[V+1]][neighbours] (+ the in-lists if directed)."""
+    def block(lists):
+        off = np.zeros(V + 1, dtype=np.int64)
+        off[1:] = np.cumsum([len(l) for l in lists])
+        if weighted:
+            nb = np.array([x for l in lists for pair in l for x in pair], dtype=np.int32)
+        else:
+            nb = np.array([x for l in lists for x in l], dtype=np.int32)
+        return off.tobytes() + nb.tobytes()
+    E = sum(len(l) for l in out_lists)
+    data = bytes([1 if directed else 0]) + np.int64(E).tobytes() + np.int64(V).tobytes() + block(out_lists)
+    if directed:
+        data += block(in_lists)
+    path.write_bytes(data)
+
+
+def test_gapbs_serialized_graphs_by_hand(tmp_path):
+    # directed 0->1, 0->2, 2->1 ; in-lists 1:{0,2} 2:{0}
+    _gapbs_sg(tmp_path / "d.sg", True, 3, [[1, 2], [], [1]], [[], [0, 2], [0]])
+    g = HostGraph.load(str(tmp_path / "d.sg"))
+    np.testing.assert_array_equal(g.offsets, [0, 2, 2, 3])
+    np.testing.assert_array_equal(g.dst, [1, 2, 1])
+    np.testing.assert_array_equal(g.weights, [1, 1, 1])
+    _gapbs_sg(tmp_path / "u.wsg", False, 3, [[(1, 7)], [(0, 7), (2, 4)], [(1, 4)]], weighted=True)
+    g = HostGraph.load(str(tmp_path / "u.wsg"))
+    np.testing.assert_array_equal(g.offsets, [0, 1, 3, 4])
+    np.testing.assert_array_equal(g.dst, [1, 0, 2, 1])
+    np.testing.assert_array_equal(g.weights, [7, 7, 4, 4])
+
+
+@pytest.mark.parametrize("suffix,directed", [(".sg", True), (".wsg", True), (".wsg", False)])
+def test_gapbs_serialized_roundtrip(tmp_path, suffix, directed):
+    hg = HostGraph.rmat(9, 8, symmetrize=not directed)
+    p = tmp_path / ("g" + suffix)
+    hg.save_sg(str(p), directed=directed)
+    back = HostGraph.load(str(p))
+    np.testing.assert_array_equal(back.offsets, hg.offsets)
+    np.testing.assert_array_equal(back.dst, hg.dst)
+    if suffix == ".wsg":
+        np.testing.assert_array_equal(back.weights, hg.weights)
+    else:
+        assert np.all(back.weights == 1)
+    raw = p.read_bytes()
+    assert raw[0] == int(directed)
+    V, E = hg.num_vertices, hg.num_edges
+    nb = 8 if suffix == ".wsg" else 4
+    assert len(raw) == 17 + (8 * (V + 1) + nb * E) * (2 if directed else 1)
+    if directed:  # the stored in-lists are the transpose
+        o = 17 + 8 * (V + 1) + nb * E
+        in_off = np.frombuffer(raw, dtype=np.int64, count=V + 1, offset=o)
+        np.testing.assert_array_equal(np.diff(in_off), np.bincount(hg.dst, minlength=V))
+
+
+def test_gapbs_serialized_truncated_and_corrupt(tmp_path):
+    hg = HostGraph.rmat(8, 4)
+    p = tmp_path / "g.sg"
+    hg.save_sg(str(p), directed=False)
+    data = p.read_bytes()
+    (tmp_path / "t.sg").write_bytes(data[:-4])
+    with pytest.raises(L.GGError) as e:
+        HostGraph.load(str(tmp_path / "t.sg"))
+    assert e.value.status == L.GG_ERR_IO
+    bad = bytearray(data)
+    V = hg.num_vertices
+    o = 17 + 8 * (V + 1)
+    bad[o:o + 4] = np.int32(V + 5).tobytes()  # first neighbour out of range
+    (tmp_path / "c.sg").write_bytes(bytes(bad))
+    with pytest.raises(L.GGError) as e:
+        HostGraph.load(str(tmp_path / "c.sg"))
+    assert e.value.status == L.GG_ERR_IO
+    bad = bytearray(data)
+    bad[17 + 8:17 + 16] = np.int64(10**9).tobytes()  # offsets not monotone
+    (tmp_path / "m.sg").write_bytes(bytes(bad))
+    with pytest.raises(L.GGError) as e:
+        HostGraph.load(str(tmp_path / "m.sg"))
+    assert e.value.status == L.GG_ERR_IO
+
+
 def test_text_readers(tmp_path):
     (tmp_path / "a.el").write_text("0 1\n1 2\n2 0\n1 1\n0 1\n")
     g = HostGraph.load(str(tmp_path / "a.el"))

@@ -15,6 +15,33 @@ def _g(golden, name):
     return np.array(hg.offsets), np.array(hg.dst), np.array(hg.weights)
 
 
+GOLDEN_GRAPHS = {"rmat10_k16_sym": (10, 16, True), "rmat11_k8_dir": (11, 8, False),
+                 "rmat12_k16_dir": (12, 16, False), "rmat12_k16_sym": (12, 16, True),
+                 "rmat14_k16_dir": (14, 16, False)}
+
+
+@pytest.mark.parametrize("name", sorted(GOLDEN_GRAPHS))
+def test_oracle_rmat_generator_matches_reference_builder(golden, name):
+    """The oracle's own restatement of GAPBS's generator and builder (used by the
+    benchmark's CPU legs) against the CSR digests made by the reference's code."""
+    import hashlib
+    scale, deg, sym = GOLDEN_GRAPHS[name]
+    off, dst, w = oracle.rmat(scale, deg, sym)
+    assert len(off) - 1 == int(golden[f"graph/{name}/V"])
+    assert len(dst) == int(golden[f"graph/{name}/E"])
+    h = hashlib.sha256()
+    for a in (off, dst, w):
+        h.update(np.ascontiguousarray(a, dtype=np.int32).tobytes())
+    assert h.hexdigest() == str(golden[f"graph/{name}/sha256"])
+
+
+def test_oracle_rmat_small_full_arrays(golden):
+    off, dst, w = oracle.rmat(10, 16, True)
+    np.testing.assert_array_equal(off, golden["graph_small/offsets"])
+    np.testing.assert_array_equal(dst, golden["graph_small/dst"])
+    np.testing.assert_array_equal(w, golden["graph_small/w"])
+
+
 @pytest.mark.parametrize("name", ["rmat10_k16_sym", "rmat12_k16_dir"])
 @pytest.mark.parametrize("delta", DELTAS)
 def test_sssp_oracles_match_reference(golden, name, delta):
