@@ -23,6 +23,7 @@
 
 #include "batch.h"
 #include "lb.cuh"
+#include "selector.h"
 
 namespace gg {
 
@@ -45,25 +46,67 @@ __device__ __forceinline__ void ms_depths(const MsBfsState &st, int32_t v, uint6
   }
 }
 
+// Adds the out-degree of v, entering the next level's queue, to the CTA's
+// statistics of that frontier.
+__device__ __forceinline__ void ms_note(const MsBfsState &st, unsigned long long *s_stat, int32_t v) {
+  const unsigned long long d = (unsigned long long)(__ldg(st.off + v + 1) - __ldg(st.off + v));
+  atomicAdd(s_stat, d);
+  atomicAdd(s_stat + 1, d * d);
+  atomicMax(s_stat + 2, d);
+}
+
 __global__ void __launch_bounds__(512) k_msbfs(DGraph g, MsBfsState st) {
   extern __shared__ int4 smem[];
   __shared__ unsigned long long s_act;
+  __shared__ unsigned long long s_stat[3];
   const int32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int32_t nthreads = gridDim.x * blockDim.x;
   const int32_t lane = threadIdx.x & 31;
   LoopClock clk;
   clk.start(st.loop_limit_ns);
   int32_t L = 0, bu_levels = 0;
+  double vis_v = 0, vis_e = 0;  // running totals of the frontiers so far (the same in every CTA)
   for (;; ++L) {
     const int32_t n = *(volatile int32_t *)(st.cnt4 + (L & 3));
     if (n == 0 || stopped(st.stop, st.err)) break;
+    const volatile unsigned long long *ls = st.lstat + 4 * (L % 3);
+    const double sd = (double)ls[0], sd2 = (double)ls[1], mx = (double)ls[2];
     if (tid == 0) {
       st.cnt4[(L + 2) & 3] = 0;
       st.actm[(L + 2) % 3] = 0ull;
+      for (int i = 0; i < 4; ++i) st.lstat[4 * ((L + 2) % 3) + i] = 0ull;
     }
-    if (threadIdx.x == 0) s_act = 0ull;
+    if (threadIdx.x == 0) {
+      s_act = 0ull;
+      s_stat[0] = s_stat[1] = s_stat[2] = 0ull;
+    }
+    // direction of this level: forced, the network's, or the bu_div rule
+    bool bu;
+    if (st.force_dir >= 0) {
+      bu = st.force_dir == 1;
+    } else if (st.sel || st.feat_log) {
+      float *x = reinterpret_cast<float *>(smem);  // scratch until the level's TWCE bins
+      if (threadIdx.x == 0)
+        msbfs_features(x, (double)n, sd, sd2, mx, vis_v, vis_e, L, (double)st.V, (double)st.E);
+      __syncthreads();
+      bu = st.sel ? selector_pull(st.sel, x, x + 16) : (st.bu_div > 0 && (int64_t)n * st.bu_div > st.V);
+    } else {
+      bu = st.bu_div > 0 && (int64_t)n * st.bu_div > st.V;
+    }
+    if (st.feat_log && L < st.max_log && blockIdx.x == 0 && threadIdx.x == 0) {
+      const float *x = reinterpret_cast<const float *>(smem);
+      if (!(st.force_dir >= 0))
+        for (int i = 0; i < kSelectorFeatures; ++i) st.feat_log[L * kSelectorFeatures + i] = x[i];
+      st.time_log[L] = globaltimer_ns();
+    }
+    if (st.force_dir >= 0 && st.feat_log && L < st.max_log && blockIdx.x == 0 && threadIdx.x == 0) {
+      float x[kSelectorFeatures];
+      msbfs_features(x, (double)n, sd, sd2, mx, vis_v, vis_e, L, (double)st.V, (double)st.E);
+      for (int i = 0; i < kSelectorFeatures; ++i) st.feat_log[L * kSelectorFeatures + i] = x[i];
+    }
+    vis_v = fmin((double)st.V, vis_v + n);
+    vis_e = fmin((double)st.E, vis_e + sd);
     __syncthreads();
-    const bool bu = st.bu_div > 0 && (int64_t)n * st.bu_div > st.V;
     const uint64_t *frc = ms_fr(st, L);
     uint64_t *frn = ms_fr(st, L + 1);
     int32_t *qn = ms_q(st, L + 1);
@@ -111,6 +154,7 @@ __global__ void __launch_bounds__(512) k_msbfs(DGraph g, MsBfsState st) {
             else
               atomicOr(st.err, DEV_ERR_OVERFLOW);
             atomicOr(&s_act, (unsigned long long)found);
+            ms_note(st, s_stat, v);
           }
           ms_depths(st, v, found, L + 1, sub, 8);
         }
@@ -129,6 +173,7 @@ __global__ void __launch_bounds__(512) k_msbfs(DGraph g, MsBfsState st) {
         frn[v] = nb;
         st.acc[v] = 0;
         atomicOr(&s_act, (unsigned long long)nb);
+        ms_note(st, s_stat, v);
         ms_depths(st, v, nb, L + 1, 0, 1);
       }
     }
@@ -140,13 +185,22 @@ __global__ void __launch_bounds__(512) k_msbfs(DGraph g, MsBfsState st) {
       for (int32_t i = tid; i < m; i += nthreads) old[__ldcg(qo + i)] = 0ull;
     }
     __syncthreads();
-    if (threadIdx.x == 0 && s_act) atomicOr(st.actm + (L + 1) % 3, s_act);
+    if (threadIdx.x == 0) {
+      if (s_act) atomicOr(st.actm + (L + 1) % 3, s_act);
+      unsigned long long *nx = st.lstat + 4 * ((L + 1) % 3);  // statistics of the next frontier
+      if (s_stat[0]) {
+        atomicAdd(nx, s_stat[0]);
+        atomicAdd(nx + 1, s_stat[1]);
+        atomicMax(nx + 2, s_stat[2]);
+      }
+    }
     clk.tick(st.stop);
     if (!grid_barrier(st.bar, gridDim.x, st.err, st.timeout_ns)) break;
   }
   if (tid == 0) {
     st.stats[0] = L;
     st.stats[1] = bu_levels;
+    if (st.time_log && L <= st.max_log) st.time_log[L] = globaltimer_ns();
   }
 }
 
@@ -181,6 +235,13 @@ __global__ void k_msbfs_seed(MsBfsState st, const int32_t *__restrict__ srcs) {
   }
   for (int i = 0; i < 4; ++i) st.cnt4[i] = 0;
   st.cnt4[0] = n;
+  for (int i = 0; i < 12; ++i) st.lstat[i] = 0ull;
+  for (int32_t i = 0; i < n; ++i) {  // the sources' frontier
+    const unsigned long long d = (unsigned long long)(st.off[st.q[0][i] + 1] - st.off[st.q[0][i]]);
+    st.lstat[0] += d;
+    st.lstat[1] += d * d;
+    st.lstat[2] = st.lstat[2] > d ? st.lstat[2] : d;
+  }
   st.actm[0] = all;
   st.actm[1] = 0;
   st.actm[2] = 0;
@@ -198,7 +259,7 @@ gg_status msbfs_buffers(gg_graph *g, int32_t nsrc, bool owned, MsBfsBuffers *b) 
   GG_TRY(ensure_transpose(g));  // in-lists for the bottom-up levels
   const int32_t V = g->csr.V;
   b->owned = owned;
-  const size_t sz[3] = {sizeof(uint64_t) * (5 * (size_t)V + 8), sizeof(int32_t) * (4 * (size_t)V + 64),
+  const size_t sz[3] = {sizeof(uint64_t) * (5 * (size_t)V + 24), sizeof(int32_t) * (4 * (size_t)V + 64),
                         sizeof(int32_t) * (size_t)std::max(nsrc, kMsBfsWidth)};
   void **ptr[3] = {(void **)&b->masks, (void **)&b->ints, (void **)&b->dsrc};
   for (int i = 0; i < 3; ++i) {
@@ -218,6 +279,7 @@ MsBfsState msbfs_state(gg_graph *g, const MsBfsBuffers &b, int32_t k, int32_t *d
   S.acc = b.masks + V;
   for (int i = 0; i < 3; ++i) S.fr[i] = b.masks + (2 + i) * (size_t)V;
   S.actm = reinterpret_cast<unsigned long long *>(b.masks + 5 * (size_t)V);
+  S.lstat = reinterpret_cast<unsigned long long *>(b.masks + 5 * (size_t)V + 8);
   S.qstamp = b.ints;
   for (int i = 0; i < 3; ++i) S.q[i] = b.ints + (1 + i) * (size_t)V;
   int32_t *hdr = b.ints + 4 * (size_t)V;
@@ -236,6 +298,10 @@ MsBfsState msbfs_state(gg_graph *g, const MsBfsBuffers &b, int32_t k, int32_t *d
   S.bar = g->d_bar;
   S.err = g->d_err;
   S.timeout_ns = barrier_timeout_ns();
+  S.sel = g->batch_selector[GG_BATCH_BFS] ? selector_params(g->batch_selector[GG_BATCH_BFS]) : nullptr;
+  S.force_dir = -1;
+  S.off = g->csr.off;
+  S.E = g->csr.E;
   return S;
 }
 
@@ -312,5 +378,77 @@ extern "C" gg_status gg_bfs_batch(gg_graph *g, const int32_t *sources, int32_t n
     stats->fused = 1;
     stats->launches = (int32_t)(launches() - l0);
   }
+  return GG_OK;
+}
+
+// Attaches a selector network to a graph's batched kernels (NULL detaches it).
+extern "C" gg_status gg_batch_set_selector(gg_graph *g, int32_t app, const gg_selector *sel) {
+  GG_CHECK_ARG(g, "graph is NULL");
+  if (app != GG_BATCH_BFS)
+    return set_error(GG_ERR_UNSUPPORTED, "only batched BFS takes a learned per-level choice");
+  g->batch_selector[app] = sel;
+  return GG_OK;
+}
+
+// Training data for the batched BFS direction: the first min(nsrc, 64) sources
+// traversed with every level top-down, then with every level bottom-up (twice
+// each; a level's masks after it are the same either way, so level l starts
+// from the same state in every run).  feats[l][12]: the features of level l;
+// times[l][2]: its best time in ms top-down and bottom-up.
+extern "C" gg_status gg_batch_collect(gg_graph *g, int32_t app, const int32_t *sources, int32_t nsrc,
+                                      int32_t max_rows, float *feats, float *times, int32_t *nrows) {
+  GG_CHECK_ARG(g && sources && nsrc > 0 && feats && times && nrows && max_rows > 0, "bad arguments");
+  if (app != GG_BATCH_BFS) return set_error(GG_ERR_UNSUPPORTED, "timings are collected for batched BFS");
+  const int32_t V = g->csr.V;
+  for (int32_t i = 0; i < nsrc; ++i) GG_CHECK_ARG(sources[i] >= 0 && sources[i] < V, "source out of range");
+  *nrows = 0;
+  cudaStream_t st = g->stream;
+  const int32_t k = std::min(nsrc, kMsBfsWidth);
+  MsBfsBuffers b;
+  GG_TRY(msbfs_buffers(g, k, false, &b));
+  int32_t *depth = nullptr;
+  GG_TRY(scratch_get_app(g, 3, sizeof(int32_t) * (size_t)k * V, (void **)&depth));
+  float *dfeat = nullptr;
+  unsigned long long *dtime = nullptr;
+  GG_CUDA(dev_alloc(&dfeat, sizeof(float) * kSelectorFeatures * (size_t)max_rows, st));
+  GG_CUDA(dev_alloc(&dtime, sizeof(unsigned long long) * ((size_t)max_rows + 1), st));
+  std::vector<float> best(2 * (size_t)max_rows, INFINITY);
+  std::vector<unsigned long long> ht((size_t)max_rows + 1);
+  int32_t levels = -1;
+  gg_status status = GG_OK;
+  for (int rep = 0; rep < 4 && status == GG_OK; ++rep) {
+    const int dir = rep & 1;
+    MsBfsState S = msbfs_state(g, b, k, depth);
+    S.force_dir = dir;
+    S.feat_log = dfeat;
+    S.time_log = dtime;
+    S.max_log = max_rows;
+    if (cudaMemcpyAsync(b.dsrc, sources, sizeof(int32_t) * k, cudaMemcpyDefault, st) != cudaSuccess ||
+        (status = msbfs_enqueue(g, st, S, b.dsrc, false)) != GG_OK)
+      break;
+    int32_t lv = 0;
+    if (cudaMemcpyAsync(&lv, S.stats, sizeof(int32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+      status = set_error(GG_ERR_CUDA, "batched BFS timing run failed");
+      break;
+    }
+    if ((status = check_device_error(g, "batch_collect")) != GG_OK) break;
+    if (levels >= 0 && lv != levels) {
+      status = set_error(GG_ERR_STATE, "level counts differ between direction runs (%d, %d)", levels, lv);
+      break;
+    }
+    levels = lv;
+    const int32_t rows = std::min(levels, max_rows);
+    cudaMemcpy(ht.data(), dtime, sizeof(unsigned long long) * ((size_t)rows + 1), cudaMemcpyDeviceToHost);
+    for (int32_t l = 0; l < rows; ++l)
+      best[2 * l + dir] = std::min(best[2 * l + dir], (float)((double)(ht[l + 1] - ht[l]) * 1e-6));
+    if (rep == 0)
+      cudaMemcpy(feats, dfeat, sizeof(float) * kSelectorFeatures * (size_t)rows, cudaMemcpyDeviceToHost);
+  }
+  cudaFreeAsync(dfeat, st);
+  cudaFreeAsync(dtime, st);
+  GG_TRY(status);
+  *nrows = std::min(levels, max_rows);
+  for (int32_t i = 0; i < 2 * *nrows; ++i) times[i] = best[i];
   return GG_OK;
 }

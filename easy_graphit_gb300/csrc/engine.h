@@ -62,6 +62,7 @@ struct gg_graph {
   gg_pq *app_pq = nullptr;
   gg_frontier_list *app_list = nullptr;
   gg_batch_tuning tuning[3] = {};  // batched BFS, SSSP, BC launch shapes (0 = default)
+  const gg_selector *batch_selector[3] = {};  // learned per-level choices of the batched kernels
 };
 
 struct gg_frontier {

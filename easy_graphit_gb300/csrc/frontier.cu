@@ -562,6 +562,8 @@ gg_status gg_frontier_create(gg_graph *g, int32_t init_all, gg_frontier **out) {
 
 gg_status gg_frontier_destroy(gg_frontier *f) {
   if (!f) return GG_OK;
+  if (f->owned_by_pq)
+    return set_error(GG_ERR_STATE, "the frontier belongs to a priority queue; gg_pq_destroy releases it");
   cudaStream_t st = f->g->stream;
   for (void *p : {(void *)f->q_in, (void *)f->q_out, (void *)f->cnt, (void *)f->bm_in,
                   (void *)f->bm_out, (void *)f->by_in, (void *)f->by_out, (void *)f->dedup})

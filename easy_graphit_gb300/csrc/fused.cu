@@ -154,7 +154,8 @@ struct BqArgs {
   int32_t *err;
   uint64_t timeout_ns, loop_limit_ns;
   int32_t delta;
-  int32_t solo_max;     // largest step CTA 0 runs alone
+  int32_t solo_max;     // largest relax step (frontier entries) CTA 0 runs alone
+  int32_t solo_pile_max;  // largest pile step (pile entries) CTA 0 runs alone
   int32_t fill_target;  // low-pile entries a refill aims for
   int32_t width0;       // first horizon width, in buckets
 };
@@ -177,6 +178,12 @@ static_assert(sizeof(BqLoop) == kBqLoopInts * sizeof(int32_t), "BqLoop is publis
 struct BqStep {
   int32_t kind, work, m;
 };
+
+// Small enough for CTA 0 alone: frontier entries of a relax, pile entries of
+// the other steps (one load and a compare each).
+__device__ __forceinline__ bool bq_small(const BqStep &st, const BqArgs &a) {
+  return st.work <= (st.kind == BQ_RELAX ? a.solo_max : a.solo_pile_max);
+}
 
 // The next step (pure: every CTA computes the same one).
 __device__ __forceinline__ BqStep bq_decide(const BqLoop &s, const int32_t *ctl, int32_t delta) {
@@ -204,10 +211,11 @@ __device__ __forceinline__ BqStep bq_decide(const BqLoop &s, const int32_t *ctl,
 }
 
 // One step, CTA `rank` of `nparts` taking its share.
+// `ctl` holds the control words: global memory in grid mode, CTA 0's shared
+// copy in a one-CTA session.
 template <int LB>
-__device__ __forceinline__ void bq_step(BqLoop &s, const BqArgs &a, const BqStep &st, int32_t rank,
-                                        int32_t nparts, int4 *smem, int32_t *red) {
-  int32_t *ctl = a.b.ctl;
+__device__ __forceinline__ void bq_step(BqLoop &s, const BqArgs &a, const BqStep &st, int32_t *ctl,
+                                        int32_t rank, int32_t nparts, int4 *smem, int32_t *red) {
   const bool lead = rank == 0 && threadIdx.x == 0;
   if (lead) {
     ctl[BQ_NEAR + (s.it + 1) % 3] = 0;
@@ -316,14 +324,18 @@ __device__ __forceinline__ void bq_publish(const BqLoop &s, int32_t *ctl) {
 }
 
 // CTA 0 alone: steps while they stay small (see above), then publishes the
-// loop state.  The whole CTA calls it.
+// loop state.  The control words live in shared memory for the session (every
+// count, minimum and decision is then an SM-local access) and go back to
+// global memory at its end.  The whole CTA calls it.
 template <int LB>
 __device__ __forceinline__ void bq_solo(BqLoop &s, const BqArgs &a, BqStep st, int4 *smem, int32_t *red,
-                                        int32_t *flag) {
+                                        int32_t *flag, int32_t *sctl) {
+  for (int i = threadIdx.x; i < BQ_STOP; i += blockDim.x) sctl[i] = __ldcg(a.b.ctl + i);
   uint64_t t0 = 0;
   if (threadIdx.x == 0) t0 = globaltimer_ns();
+  __syncthreads();
   for (;;) {
-    bq_step<LB>(s, a, st, 0, 1, smem, red);
+    bq_step<LB>(s, a, st, sctl, 0, 1, smem, red);
     __syncthreads();
     if (threadIdx.x == 0)
       *flag = (*(volatile int32_t *)a.err & DEV_ERR_OVERFLOW) != 0 || globaltimer_ns() - t0 > kSoloSliceNs;
@@ -331,9 +343,11 @@ __device__ __forceinline__ void bq_solo(BqLoop &s, const BqArgs &a, BqStep st, i
     const bool quit = *flag != 0;
     __syncthreads();
     if (quit) break;
-    st = bq_decide(s, a.b.ctl, a.delta);
-    if (st.kind == BQ_DONE || st.work > a.solo_max) break;
+    st = bq_decide(s, sctl, a.delta);
+    if (st.kind == BQ_DONE || !bq_small(st, a)) break;
   }
+  for (int i = threadIdx.x; i < BQ_STOP; i += blockDim.x) a.b.ctl[i] = sctl[i];
+  __syncthreads();
   bq_publish(s, a.b.ctl);
 }
 
@@ -341,6 +355,7 @@ template <int LB>
 __global__ void __launch_bounds__(1024) k_sssp_bq(BqArgs a) {
   extern __shared__ int4 smem[];
   __shared__ int32_t red[33];
+  __shared__ int32_t sctl[BQ_STOP];  // counts and minima of a one-CTA session
   BqLoop s{1, 0, 0, 0, 0, bq_clamp((int64_t)a.width0 * a.delta), a.width0, 0, 0, 0};
   int32_t *stop = a.b.ctl + BQ_STOP;
   LoopClock clk;
@@ -352,12 +367,12 @@ __global__ void __launch_bounds__(1024) k_sssp_bq(BqArgs a) {
       if (s.phase == 0) s.adv++;  // the reference's last advance finds no priority left
       break;
     }
-    if (st.work <= a.solo_max) {
+    if (bq_small(st, a)) {
       // CTA 0 starts changing the control words only once every other CTA
       // has taken its decision from them and arrived at the barrier.
       if (blockIdx.x == 0) {
         if (grid_wait_others(a.bar, gridDim.x, a.err, a.timeout_ns))
-          bq_solo<LB>(s, a, st, smem, red, red + 32);
+          bq_solo<LB>(s, a, st, smem, red, red + 32, sctl);
         else
           bq_publish(s, a.b.ctl);
       }
@@ -368,7 +383,7 @@ __global__ void __launch_bounds__(1024) k_sssp_bq(BqArgs a) {
       for (int i = 0; i < kBqLoopInts; ++i) p[i] = pub[i];
       continue;
     }
-    bq_step<LB>(s, a, st, blockIdx.x, gridDim.x, smem, red);
+    bq_step<LB>(s, a, st, a.b.ctl, blockIdx.x, gridDim.x, smem, red);
     clk.tick(stop);
     if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
   }
@@ -485,14 +500,16 @@ gg_status fused_bfs(gg_graph *g, const gg_schedule *s, int32_t n0, const VData &
   return GG_OK;
 }
 
-// Largest step the SSSP loop runs on one CTA (GG_BQ_SOLO_MAX overrides; 0
-// turns the one-CTA mode off).
-static int32_t bq_solo_max(int cta) {
+// Largest relax step the SSSP loop runs on one CTA, in frontier entries per
+// thread of the CTA (GG_BQ_SOLO_PER_THREAD overrides; 0 turns the one-CTA
+// mode off).  Pile steps take 8 times as many entries: one load and a
+// compare each.
+static int32_t bq_solo_per_thread() {
   static const long env = [] {
-    const char *e = getenv("GG_BQ_SOLO_MAX");
+    const char *e = getenv("GG_BQ_SOLO_PER_THREAD");
     return e ? atol(e) : -1L;
   }();
-  return env >= 0 ? (int32_t)env : 2 * cta;
+  return env >= 0 ? (int32_t)env : 4;
 }
 
 static BqArgs bq_args(gg_graph *g, gg_frontier *f, const BqBuffers &b, int32_t *dist, int32_t delta, int cta) {
@@ -509,8 +526,9 @@ static BqArgs bq_args(gg_graph *g, gg_frontier *f, const BqBuffers &b, int32_t *
   a.timeout_ns = barrier_timeout_ns();
   a.loop_limit_ns = loop_timeout_ns();
   a.delta = delta;
-  a.solo_max = bq_solo_max(cta);
-  a.fill_target = 4096;
+  a.solo_max = bq_solo_per_thread() * cta;
+  a.solo_pile_max = 8 * a.solo_max;
+  a.fill_target = 1024;
   a.width0 = 16;
   return a;
 }

@@ -17,6 +17,8 @@
 //  - every call shares the one array and it keeps the previous call's contents:
 //    each call re-initialises the parts that must start at zero, and calls that
 //    overlap on the GPU (different streams, or another thread) race on it.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "engine.h"
@@ -30,9 +32,15 @@ constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) int32_t g_noalloc_scratch[kNoAllocHeader + 2 * kNoAllocMaxVertices];
 
-// Host copies of the array's device address, one per device, filled by the
-// first call on that device (with the device current).
-static int32_t *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+// Host copies of the array's device address, one per device, each tagged with
+// the unique id of the context it was looked up in: the array lives in the
+// module loaded into that context, so after cudaDeviceReset, or under another
+// context made current by the caller, the address is looked up again.
+struct NoAllocSlot {
+  unsigned long long ctx_id = 0;
+  int32_t *ptr = nullptr;
+};
+static NoAllocSlot g_noalloc_slot[kNoAllocMaxDevices];
 static std::mutex g_noalloc_mu;
 
 // BFS UDF on the output array itself: depth[v] == -1 marks unvisited, and the
@@ -96,23 +104,59 @@ __global__ void __launch_bounds__(512) k_noalloc_bfs(DGraph g, int32_t *scratch,
   if (blockIdx.x == 0 && threadIdx.x == 0) scratch[6] = (int32_t)(level - 1);
 }
 
-// Device address of the scratch array on the current device (set-up on the
-// first call per device).
+// Unique id of the calling thread's current context (0 when none is current
+// yet), through the driver entry points the runtime hands out (no libcuda link).
+static gg_status current_context_id(unsigned long long *id) {
+  using GetCurrent = CUresult (*)(CUcontext *);
+  using GetId = CUresult (*)(CUcontext, unsigned long long *);
+  struct Entry {
+    GetCurrent get_current = nullptr;
+    GetId get_id = nullptr;
+  };
+  static const Entry fn = [] {  // resolved once (thread-safe static initialisation)
+    Entry e;
+    void *a = nullptr, *b = nullptr;
+    cudaDriverEntryPointQueryResult qa{}, qb{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+        qa == cudaDriverEntryPointSuccess && qb == cudaDriverEntryPointSuccess) {
+      e.get_current = reinterpret_cast<GetCurrent>(a);
+      e.get_id = reinterpret_cast<GetId>(b);
+    }
+    return e;
+  }();
+  if (!fn.get_current || !fn.get_id)
+    return set_error(GG_ERR_CUDA, "driver entry points cuCtxGetCurrent / cuCtxGetId not found");
+  CUcontext ctx = nullptr;
+  if (fn.get_current(&ctx) != CUDA_SUCCESS) return set_error(GG_ERR_CUDA, "cuCtxGetCurrent failed");
+  *id = 0;
+  if (ctx && fn.get_id(ctx, id) != CUDA_SUCCESS) return set_error(GG_ERR_CUDA, "cuCtxGetId failed");
+  return GG_OK;
+}
+
+// Device address of the scratch array in the current context of the current
+// device.  Set-up on the first call per device and context: cudaGetSymbolAddress
+// (which loads the module into the context if it is not loaded yet).
 static gg_status noalloc_scratch(int32_t **out) {
   int dev = 0;
   GG_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kNoAllocMaxDevices)
     return set_error(GG_ERR_UNSUPPORTED, "device %d beyond the %d supported", dev, kNoAllocMaxDevices);
+  unsigned long long id = 0;
+  GG_TRY(current_context_id(&id));
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
+  NoAllocSlot &slot = g_noalloc_slot[dev];
+  if (!slot.ptr || id == 0 || slot.ctx_id != id) {
     int32_t *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
     if (e != cudaSuccess)
       return set_error(GG_ERR_CUDA, "cudaGetSymbolAddress of the no-alloc scratch failed: %s",
                        cudaGetErrorString(e));
-    g_noalloc_ptr[dev] = p;
+    if (id == 0) GG_TRY(current_context_id(&id));  // the lookup made the primary context current
+    slot.ptr = p;
+    slot.ctx_id = id;
   }
-  *out = g_noalloc_ptr[dev];
+  *out = slot.ptr;
   return GG_OK;
 }
 

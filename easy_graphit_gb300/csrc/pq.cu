@@ -224,6 +224,7 @@ gg_status gg_pq_create(gg_graph *g, int32_t *priorities, int32_t init_priority, 
   if (s == GG_OK) s = pq_reset(pq, init_priority, delta, src);
   if (s != GG_OK) {
     bq_free(g, &pq->bq);
+    pq->frontier->owned_by_pq = false;
     gg_frontier_destroy(pq->frontier);
     delete pq;
     return s;
@@ -235,6 +236,7 @@ gg_status gg_pq_create(gg_graph *g, int32_t *priorities, int32_t init_priority, 
 gg_status gg_pq_destroy(gg_pq *pq) {
   if (!pq) return GG_OK;
   bq_free(pq->g, &pq->bq);
+  pq->frontier->owned_by_pq = false;
   gg_frontier_destroy(pq->frontier);
   delete pq;
   return GG_OK;

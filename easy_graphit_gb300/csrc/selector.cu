@@ -27,10 +27,10 @@
 
 namespace gg {
 
-// Parameter layout (fp32): W1[16][64] b1[64] W2[64][64] b2[64] W3[64][16] b3[16]
-constexpr int kIn = 16, kH = 64, kOut = 16;
-constexpr int oW1 = 0, oB1 = oW1 + kIn * kH, oW2 = oB1 + kH, oB2 = oW2 + kH * kH, oW3 = oB2 + kH,
-              oB3 = oW3 + kH * kOut, kParams = oB3 + kOut;
+// Parameter layout: selector.h (W1[16][64] b1[64] W2[64][64] b2[64] W3[64][16] b3[16]).
+constexpr int kIn = kSelIn, kH = kSelHidden, kOut = kSelOut;
+constexpr int oW1 = kSelW1, oB1 = kSelB1, oW2 = kSelW2, oB2 = kSelB2, oW3 = kSelW3, oB3 = kSelB3,
+              kParams = oB3 + kOut;
 constexpr int kTileS = 64;  // samples per block
 
 static_assert(kParams == kSelectorParams, "parameter count");
@@ -423,6 +423,8 @@ gg_status selector_forward_device(const gg_selector *s, const float *x_dev, int3
   GG_CUDA(cudaGetLastError());
   return GG_OK;
 }
+
+const float *selector_params(const gg_selector *s) { return s->p; }
 
 // Decision for one feature vector on the device: argmax of each head.
 gg_status selector_decide(gg_selector *s, const float *x_host, int32_t decision[3], cudaStream_t st) {

@@ -1,6 +1,8 @@
 // The learned schedule selector: shared constants and internal interfaces.
 #pragma once
 
+#include <cuda_bf16.h>
+
 #include "engine.h"
 
 namespace gg {
@@ -31,5 +33,47 @@ gg_status frontier_stats(gg_graph *g, gg_frontier *f, FrontierStats *fs);
 void make_features(const gg_graph *g, const FrontierStats &fs, const RunTotals &rt, float x[kSelectorFeatures]);
 
 gg_status selector_decide(gg_selector *s, const float *x_host, int32_t decision[3], cudaStream_t st);
+// The network's fp32 master parameters on the device (layout below).
+const float *selector_params(const gg_selector *s);
+
+// Parameter layout (fp32): W1[16][64] b1[64] W2[64][64] b2[64] W3[64][16] b3[16]
+// (inputs and outputs padded to 16; the padding is zero).
+constexpr int kSelIn = 16, kSelHidden = 64, kSelOut = 16;
+constexpr int kSelW1 = 0, kSelB1 = kSelW1 + kSelIn * kSelHidden, kSelW2 = kSelB1 + kSelHidden,
+              kSelB2 = kSelW2 + kSelHidden * kSelHidden, kSelW3 = kSelB2 + kSelHidden,
+              kSelB3 = kSelW3 + kSelHidden * kSelOut;
+
+// Direction head of the network on one feature vector x (12 floats), computed
+// by the calling CTA inside a persistent kernel: fp32 accumulation over
+// bf16-rounded operands, as the tensor-core forward pass computes it.  h is
+// 2*64 floats of shared memory.  Every thread of the CTA calls it and gets the
+// same answer: true when the network picks PULL.
+__device__ __forceinline__ bool selector_pull(const float *__restrict__ p, const float *x, float *h) {
+  auto bf = [](float v) { return __bfloat162float(__float2bfloat16_rn(v)); };
+  const int j = threadIdx.x;
+  if (j < kSelHidden) {
+    float a = 0.f;
+    for (int k = 0; k < kSelectorFeatures; ++k) a += bf(x[k]) * bf(__ldg(p + kSelW1 + k * kSelHidden + j));
+    h[j] = fmaxf(a + __ldg(p + kSelB1 + j), 0.f);
+  }
+  __syncthreads();
+  if (j < kSelHidden) {
+    float a = 0.f;
+    for (int k = 0; k < kSelHidden; ++k) a += bf(h[k]) * bf(__ldg(p + kSelW2 + k * kSelHidden + j));
+    h[kSelHidden + j] = fmaxf(a + __ldg(p + kSelB2 + j), 0.f);
+  }
+  __syncthreads();
+  float z = 0.f;
+  if (j < 2) {
+    for (int k = 0; k < kSelHidden; ++k) z += bf(h[kSelHidden + k]) * bf(__ldg(p + kSelW3 + k * kSelOut + j));
+    z += __ldg(p + kSelB3 + j);
+  }
+  __syncthreads();
+  if (j < 2) h[j] = z;  // the two direction logits (push, pull)
+  __syncthreads();
+  const bool pull = h[1] > h[0];
+  __syncthreads();
+  return pull;
+}
 
 }  // namespace gg

@@ -481,9 +481,10 @@ class VertexSubset:
 
     def __del__(self):
         try:
-            if getattr(self, "_h", None):
+            # a view of a priority queue's frontier is released with the queue
+            if getattr(self, "_h", None) and getattr(self, "_owned", True):
                 lib().gg_frontier_destroy(self._h)
-                self._h = None
+            self._h = None
         except Exception:
             pass
 
@@ -799,6 +800,26 @@ def set_batch_tuning(g: GraphT, app: str, blocks_per_sm: int = 0, chunk: int = 0
     call("gg_batch_set_tuning", g.handle, BATCH_APPS[app], C.byref(t))
 
 
+def set_batch_selector(g: GraphT, app: str, selector: "Selector | None") -> None:
+    """Attaches a selector network to the graph's batched `app` kernels (batched
+    BFS: the direction of every level, decided on the device); None detaches
+    it.  The graph keeps a reference to the selector while it is attached."""
+    call("gg_batch_set_selector", g.handle, BATCH_APPS[app], selector._h if selector is not None else None)
+    g._batch_selector = selector
+
+
+def collect_batched_directions(g: GraphT, sources, max_rows: int = 1024):
+    """Per-level features [levels, 12] and times [levels, 2] (ms; top-down,
+    bottom-up) of a batched BFS over the first 64 sources."""
+    srcs = np.ascontiguousarray(sources, dtype=np.int32)
+    feats = np.empty((max_rows, N_FEATURES), dtype=np.float32)
+    times = np.empty((max_rows, 2), dtype=np.float32)
+    n = C.c_int32()
+    call("gg_batch_collect", g.handle, BATCH_APPS["bfs"], _np_ptr(srcs), len(srcs), max_rows,
+         _np_ptr(feats), _np_ptr(times), C.byref(n))
+    return feats[:n.value].copy(), times[:n.value].copy()
+
+
 def get_batch_tuning(g: GraphT, app: str) -> dict:
     t = L.gg_batch_tuning()
     call("gg_batch_get_tuning", g.handle, BATCH_APPS[app], C.byref(t))
@@ -900,6 +921,13 @@ class Selector:
         """The model shipped with the package (selector_model.bin, trained by
         easy_graphit_gb300.selector_train; its manifest is selector_model.json)."""
         return cls.load(str(Path(__file__).resolve().parent / "selector_model.bin"))
+
+    @classmethod
+    def pretrained_batched_bfs(cls) -> "Selector":
+        """The per-level direction model of batched BFS shipped with the package
+        (selector_batched_bfs.bin, trained by `easy_graphit_gb300.selector_train
+        --batched-bfs`; manifest selector_batched_bfs.json)."""
+        return cls.load(str(Path(__file__).resolve().parent / "selector_batched_bfs.bin"))
 
     def save(self, path: str) -> None:
         call("gg_selector_save", self._h, str(path).encode())

@@ -1,6 +1,15 @@
 """Trains the learned schedule selector on timings generated by the engine.
 
     python -m easy_graphit_gb300.selector_train [--out easy_graphit_gb300/selector_model.bin]
+    python -m easy_graphit_gb300.selector_train --batched-bfs [--out .../selector_batched_bfs.bin]
+
+--batched-bfs trains the per-level direction of the batched BFS instead: on
+each training graph, 64 sources are traversed with every level top-down and
+then bottom-up (gg_batch_collect); a level's label is its faster direction, and
+levels where the two differ more weigh more (the row is repeated).  The model
+runs on the device inside the batched kernel (gg_batch_set_selector); held-out
+seeds compare it with both fixed directions, the built-in rule and the
+per-level optimum.
 
 Training graphs: R-MAT at scales 18 to 24 with skew a in [0.45, 0.75] (b = c =
 (0.95 - a) / 2) and 2-D grids, GAPBS-seeded; for each, BFS and SSSP runs
@@ -21,11 +30,13 @@ from pathlib import Path
 
 import numpy as np
 
-from .graphit import (GraphT, HostGraph, LearnedGPUSchedule, Selector, bfs, cc, collect_timings,
-                      default_schedule, labels_from_times, sssp)
+from .graphit import (GraphT, HostGraph, LearnedGPUSchedule, Selector, bfs, bfs_batch, cc,
+                      collect_batched_directions, collect_timings, default_schedule, labels_from_times,
+                      set_batch_selector, set_batch_tuning, sssp)
 
 PKG = Path(__file__).resolve().parent
 DEFAULT_OUT = PKG / "selector_model.bin"
+BATCHED_BFS_OUT = PKG / "selector_batched_bfs.bin"
 
 TRAIN_SEEDS = [101, 102, 103]
 HELDOUT_SEEDS = [901, 902]
@@ -108,8 +119,117 @@ def evaluate(model, scale, log):
     return rows
 
 
+# ------------------------------------------------------------ batched BFS
+def collect_batched_bfs(scales, skews, grids, log):
+    X, T = [], []
+    for name, scale, a, seed in training_graphs(scales, skews):
+        for sym in (True, False):
+            hg = rmat(scale, a, seed, sym)
+            g = GraphT(hg, symmetric=sym)
+            for grp in range(2):
+                f, t = collect_batched_directions(g, hg.pick_sources(64, seed=seed + 17 * grp))
+                X.append(f)
+                T.append(t)
+                log(f"{name}{' sym' if sym else ''} group {grp}: {len(f)} levels, "
+                    f"top-down {t[:, 0].sum():.2f} ms, bottom-up {t[:, 1].sum():.2f} ms, best {t.min(1).sum():.2f} ms")
+            g.close()
+    for n in grids:
+        hg = HostGraph.grid(n, n, seed=TRAIN_SEEDS[0])
+        g = GraphT(hg, symmetric=True)
+        f, t = collect_batched_directions(g, hg.pick_sources(64, seed=7))
+        X.append(f)
+        T.append(t)
+        log(f"grid{n}: {len(f)} levels")
+        g.close()
+    return np.concatenate(X), np.concatenate(T)
+
+
+def batched_rows(X, T):
+    """Labels (direction = the faster one; the other heads fixed) and rows
+    repeated by how much the choice matters (1 + 4 x the relative gap, at most 9)."""
+    lab = np.zeros((len(X), 3), dtype=np.int32)
+    lab[:, 0] = (T[:, 1] < T[:, 0]).astype(np.int32)
+    gap = np.abs(T[:, 0] - T[:, 1]) / np.maximum(T.min(1), 1e-6)
+    rep = 1 + np.minimum(8, np.floor(4 * gap)).astype(np.int64)
+    return np.repeat(X, rep, axis=0), np.repeat(lab, rep, axis=0)
+
+
+def evaluate_batched(model, log):
+    """Held-out seeds: per-level cost of each policy on the measured level times
+    (every level top-down, every level bottom-up, the network's choice, the
+    per-level optimum), and whole batched runs with the network attached against
+    top-down only and the built-in rule, depths compared."""
+    rows = []
+    for name, hg, sym in (("rmat20_sym", rmat(20, 0.57, HELDOUT_SEEDS[0], True), True),
+                          ("rmat22", rmat(22, 0.57, HELDOUT_SEEDS[1], False), False),
+                          ("rmat21_a0.65_sym", rmat(21, 0.65, HELDOUT_SEEDS[1], True), True),
+                          ("grid1024", HostGraph.grid(1024, 1024, seed=HELDOUT_SEEDS[0]), True)):
+        g = GraphT(hg, symmetric=sym)
+        srcs = hg.pick_sources(64, seed=HELDOUT_SEEDS[0])
+        f, t = collect_batched_directions(g, srcs)
+        pull = model.predict(f)[:, 0]
+        per_level = {"top_down_ms": float(t[:, 0].sum()), "bottom_up_ms": float(t[:, 1].sum()),
+                     "learned_ms": float(t[np.arange(len(t)), pull].sum()), "optimum_ms": float(t.min(1).sum())}
+
+        def run(label):
+            best, out = None, None
+            for _ in range(5):
+                out, st = bfs_batch(g, srcs)
+                best = st["loop_ms"] if best is None else min(best, st["loop_ms"])
+            return best, out
+        set_batch_tuning(g, "bfs", bottom_up_div=-1)
+        td_ms, d_td = run("top-down")
+        set_batch_tuning(g, "bfs")
+        rule_ms, d_rule = run("rule")
+        set_batch_selector(g, "bfs", model)
+        learned_ms, d_learned = run("learned")
+        set_batch_selector(g, "bfs", None)
+        if not (np.array_equal(d_td, d_rule) and np.array_equal(d_rule, d_learned)):
+            raise AssertionError(f"{name}: depths differ between policies")
+        row = {"graph": name, "V": hg.num_vertices, "E": hg.num_edges, "levels": int(len(t)),
+               "per_level_cost": per_level,
+               "runs_ms": {"top_down_only": td_ms, "builtin_rule": rule_ms, "learned": learned_ms}}
+        rows.append(row)
+        log(json.dumps(row))
+        g.close()
+    return rows
+
+
+def main_batched_bfs(a, log):
+    scales = [int(s) for s in a.scales.split(",")]
+    skews = [float(s) for s in a.skews.split(",")]
+    grids = [int(s) for s in a.grids.split(",") if s]
+    t0 = time.time()
+    X, T = collect_batched_bfs(scales, skews, grids, log)
+    Xr, lab = batched_rows(X, T)
+    log(f"collected {len(X)} levels ({len(Xr)} weighted rows) in {time.time() - t0:.1f}s")
+    model = Selector(seed=27491095)
+    loss = model.train(Xr, lab, epochs=a.epochs, lr=a.lr)
+    pull = model.predict(X)[:, 0]
+    acc = float((pull == (T[:, 1] < T[:, 0])).mean())
+    regret = float(T[np.arange(len(T)), pull].sum() / T.min(1).sum())
+    log(f"loss {loss:.4f} direction accuracy {acc:.3f} time / per-level optimum {regret:.3f}")
+    out = a.out if a.out != str(DEFAULT_OUT) else str(BATCHED_BFS_OUT)
+    model.save(out)
+    evals = evaluate_batched(model, log)
+    manifest = {
+        "file": Path(out).name, "params": int(len(model.params)),
+        "architecture": "12 -> 64 -> 64 -> 11 (bf16 MLP); the direction head picks each level's direction "
+                        "of the batched BFS, on the device; the other heads are unused",
+        "training": {"levels": int(len(X)), "weighted_rows": int(len(Xr)), "scales": scales, "skews": skews,
+                     "grids": grids, "seeds": TRAIN_SEEDS, "sources_per_graph": "2 groups of 64 (R-MAT), 64 (grids)",
+                     "epochs": a.epochs, "lr": a.lr, "final_loss": loss, "direction_accuracy": acc,
+                     "time_over_per_level_optimum": regret},
+        "heldout": evals,
+    }
+    Path(out).with_suffix(".json").write_text(json.dumps(manifest, indent=1))
+    log(json.dumps(manifest))
+
+
 def main():
     p = argparse.ArgumentParser()
+    p.add_argument("--batched-bfs", action="store_true",
+                   help="train the per-level direction of the batched BFS (selector_batched_bfs.bin)")
     p.add_argument("--out", default=str(DEFAULT_OUT))
     p.add_argument("--scales", default="18,20,22,24")
     p.add_argument("--skews", default="0.45,0.57,0.75")
@@ -120,6 +240,9 @@ def main():
     p.add_argument("--eval-scale", type=int, default=20)
     a = p.parse_args()
     log = lambda m: print(m, flush=True)
+    if a.batched_bfs:
+        main_batched_bfs(a, log)
+        return
     scales = [int(s) for s in a.scales.split(",")]
     skews = [float(s) for s in a.skews.split(",")]
     grids = [int(s) for s in a.grids.split(",") if s]

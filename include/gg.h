@@ -171,6 +171,9 @@ void gg_host_graph_destroy(gg_host_graph *g);
  * get_transposed_graph (graph.h:165-234) and get_blocked_graph
  * (graph.h:105-163) run on the GPU here and are cached in the handle. */
 typedef struct gg_graph gg_graph;
+/* GG_GRAPH_SYMMETRIC promises that every edge (u, v, w) has its reverse
+ * (v, u, w) with the same weight: the graph is then its own transpose and
+ * pull schedules use it as such. */
 enum { GG_GRAPH_SYMMETRIC = 1 };
 gg_status gg_graph_create(const int32_t *offsets, const int32_t *dst,
                           const int32_t *weights, int32_t num_vertices,
@@ -279,7 +282,8 @@ gg_status gg_pq_create(gg_graph *g, int32_t *priorities, int32_t init_priority,
                        int32_t delta, int32_t src, gg_pq **out);
 gg_status gg_pq_destroy(gg_pq *pq);
 gg_status gg_pq_finished(gg_pq *pq, int32_t *finished);
-/* dequeue(): returns the queue's frontier (owned by the queue). */
+/* dequeue(): returns the queue's frontier (owned by the queue: released by
+ * gg_pq_destroy; gg_frontier_destroy refuses it with GG_ERR_STATE). */
 gg_status gg_pq_dequeue(gg_pq *pq, gg_frontier **frontier);
 /* edgeset_apply(s).from(pq frontier).apply_priority(g, relax, pq)
  * (operators.h:73-103). */
@@ -387,11 +391,12 @@ gg_status gg_selector_collect(gg_graph *g, int32_t app, int32_t src, int32_t del
  * The library allocates nothing here: its scratch is one static device array
  * sized for at most 1,048,576 vertices (about 8 MiB, held on every GPU that
  * loads the library until the process exits); larger graphs are rejected with
- * GG_ERR_INVALID.  The first call on a device looks up that array's address, so
- * make the first call before capturing the stream into a CUDA graph.  All
- * calls share the array: calls that overlap on the GPU race and must be
- * serialised by the caller.  Runs on `stream` (NULL = legacy default stream)
- * and returns when the result is in depth_out. */
+ * GG_ERR_INVALID.  The first call on a device (and the first after the calling
+ * thread's current context changes) looks up that array's address, so make
+ * that call before any stream capture begins.  All calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller.
+ * Runs on `stream` (NULL = legacy default stream), reads its status word back
+ * and synchronises `stream` before it returns, with the result in depth_out. */
 gg_status gg_bfs_noalloc(const int32_t *offsets, const int32_t *dst,
                          int32_t num_vertices, int32_t num_edges, int32_t src,
                          int32_t *depth_out, void *stream);
@@ -479,6 +484,22 @@ gg_status gg_sssp_multi(gg_graph *g, const gg_app_schedule *s,
                         int32_t *dist_out, gg_stats *stats);
 gg_status gg_sssp_batch(gg_graph *g, const int32_t *sources, int32_t nsrc,
                         int32_t delta, int32_t *dist_out, gg_stats *stats);
+
+/* Learned per-level schedule of the batched kernels (no reference
+ * counterpart): with a selector attached, batched BFS (GG_BATCH_BFS, the only
+ * app that takes one) picks each level's direction -- top-down or bottom-up --
+ * with the network's direction head on that level's frontier statistics,
+ * computed on the device inside the persistent loop (no host round trip).
+ * NULL detaches it (the bottom_up_div rule decides again).  The selector must
+ * outlive the calls and plans that use it.  Results never depend on it. */
+gg_status gg_batch_set_selector(gg_graph *g, int32_t app, const gg_selector *sel);
+/* Its training data, made by the engine: the first min(nsrc, 64) sources
+ * traversed with every level forced top-down and then bottom-up (a level's
+ * result does not depend on its direction, so level l starts from the same
+ * state in every run).  feats[l][12] (the selector's features of level l),
+ * times[l][2] (ms top-down, bottom-up); *nrows = levels recorded. */
+gg_status gg_batch_collect(gg_graph *g, int32_t app, const int32_t *sources, int32_t nsrc,
+                           int32_t max_rows, float *feats, float *times, int32_t *nrows);
 
 /* ------------------------------------------------------------ diagnostics
  * Runs a grid barrier that can never complete (it waits for one block more

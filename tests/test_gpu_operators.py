@@ -30,7 +30,9 @@ def graph(name):
         hg = {"sym12": lambda: HostGraph.rmat(12, 16, symmetrize=True),
               "dir12": lambda: HostGraph.rmat(12, 16),
               "grid": lambda: HostGraph.grid(48, 64)}[name]()
-        sym = name != "dir12"
+        # the grid has every edge both ways but with independent weights, so it is
+        # not symmetric in the GG_GRAPH_SYMMETRIC sense (a weighted pull needs its transpose)
+        sym = name == "sym12"
         _G[name] = (GraphT(hg, symmetric=sym), np.array(hg.offsets), np.array(hg.dst), np.array(hg.weights))
     return _G[name]
 

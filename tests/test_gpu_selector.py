@@ -5,8 +5,9 @@ import pytest
 
 import oracle
 from oracle import selector_ref as ref
-from easy_graphit_gb300 import (GraphT, HostGraph, LearnedGPUSchedule, Selector, bfs, cc,
-                                collect_timings, sssp)
+from easy_graphit_gb300 import (GraphT, HostGraph, LearnedGPUSchedule, Selector, bfs, bfs_batch, cc,
+                                collect_batched_directions, collect_timings, set_batch_selector,
+                                set_batch_tuning, sssp)
 from easy_graphit_gb300.graphit import labels_from_times
 
 pytestmark = pytest.mark.gpu
@@ -166,3 +167,61 @@ def test_out_of_range_labels_are_rejected():
             s.grad(x, l2)
         with pytest.raises(Exception, match="out of range"):
             s.train(x, l2, epochs=1)
+
+
+def test_batched_bfs_direction_timings_and_device_inference():
+    """gg_batch_collect's forced-direction runs agree on the levels; the device
+    features are finite; with a selector attached the depths are unchanged."""
+    hg = HostGraph.rmat(14, 16, symmetrize=True)
+    g = GraphT(hg, symmetric=True)
+    off, dst = np.array(hg.offsets), np.array(hg.dst)
+    srcs = hg.pick_sources(64)
+    f, t = collect_batched_directions(g, srcs)
+    assert len(f) >= 3 and np.all(np.isfinite(f)) and np.all(t > 0)
+    assert f[0, 0] == np.float32(np.log2(1 + len(set(srcs.tolist()))) / 32)
+    plain, _ = bfs_batch(g, srcs)
+    set_batch_selector(g, "bfs", Selector(seed=5))  # an untrained network: any choice is exact
+    learned, _ = bfs_batch(g, srcs)
+    set_batch_selector(g, "bfs", None)
+    np.testing.assert_array_equal(learned, plain)
+    np.testing.assert_array_equal(plain[3], oracle.bfs(off, dst, int(srcs[3])))
+    g.close()
+
+
+def test_learned_batched_bfs_beats_both_fixed_directions_on_heldout_graphs():
+    """The shipped per-level direction model of batched BFS on graphs it was
+    not trained on (seeds 903, 904): on the measured level times its choices
+    cost less than either fixed direction (every level top-down / bottom-up),
+    whole runs with it attached beat top-down only, and the depths equal the
+    oracle's."""
+    model = Selector.pretrained_batched_bfs()
+    report = {}
+    for name, hg, sym in (("rmat20_sym", HostGraph.rmat(20, 16, seed=903, symmetrize=True), True),
+                          ("rmat21", HostGraph.rmat(21, 16, seed=904), False)):
+        g = GraphT(hg, symmetric=sym)
+        off, dst = np.array(hg.offsets), np.array(hg.dst)
+        srcs = hg.pick_sources(64, seed=903)
+        f, t = collect_batched_directions(g, srcs)
+        pull = model.predict(f)[:, 0]
+        cost = {"top_down": float(t[:, 0].sum()), "bottom_up": float(t[:, 1].sum()),
+                "learned": float(t[np.arange(len(t)), pull].sum())}
+        assert cost["learned"] < min(cost["top_down"], cost["bottom_up"]), (name, cost)
+
+        def best_run():
+            best, out = None, None
+            for _ in range(3):
+                out, st = bfs_batch(g, srcs)
+                best = st["loop_ms"] if best is None else min(best, st["loop_ms"])
+            return best, out
+        set_batch_tuning(g, "bfs", bottom_up_div=-1)
+        td_ms, _ = best_run()
+        set_batch_tuning(g, "bfs")
+        set_batch_selector(g, "bfs", model)
+        learned_ms, depth = best_run()
+        set_batch_selector(g, "bfs", None)
+        for i in (0, 63):
+            np.testing.assert_array_equal(depth[i], oracle.bfs(off, dst, int(srcs[i])))
+        assert learned_ms < td_ms, (name, learned_ms, td_ms)
+        report[name] = dict(cost, top_down_run_ms=td_ms, learned_run_ms=learned_ms)
+        g.close()
+    print("held-out batched BFS:", report)

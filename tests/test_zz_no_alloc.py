@@ -32,14 +32,25 @@ def test_bfs_noalloc_matches_gg_bfs_twice():
     deg = np.diff(hg.offsets)
     sources = [int(np.argmax(deg)), int(np.nonzero(deg)[0][7])]
     stream = torch.cuda.current_stream(dev)
-    for src in sources:  # two calls in a row, different sources
-        want, _, _ = bfs(g, src)
-        out = torch.full((V,), 123, dtype=torch.int32, device=dev)
+    wants = [bfs(g, src)[0] for src in sources]  # the regular entry point (which allocates)
+    import oracle
+    np.testing.assert_array_equal(wants[0], oracle.bfs(np.array(hg.offsets), np.array(hg.dst), sources[0]))
+    outs = [torch.full((V,), 123, dtype=torch.int32, device=dev) for _ in sources]
+
+    def call(src, out):
         st = L.lib().gg_bfs_noalloc(C.c_void_p(off.data_ptr()), C.c_void_p(dst.data_ptr()), V, E, src,
                                     C.c_void_p(out.data_ptr()), C.c_void_p(stream.cuda_stream))
         assert st == L.GG_OK, L.last_error()
-        got = out.cpu().numpy()
-        np.testing.assert_array_equal(got, want)  # BFS depths: exact
+
+    call(sources[0], outs[0])  # set-up: looks up the scratch array's address
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info(dev)[0]
+    for src, out, want in zip(sources, outs, wants):  # two calls in a row, different sources
+        call(src, out)
+        np.testing.assert_array_equal(out.cpu().numpy(), want)  # BFS depths: exact
+    torch.cuda.synchronize()
+    # nothing was allocated on the device by those calls
+    assert torch.cuda.mem_get_info(dev)[0] == free_before
     g.close()
 
 
