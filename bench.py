@@ -378,6 +378,7 @@ def run_gb300(args):
     apps = per_app(g, hg, off, dst, dev, stream, peaks()[0]) if lead and not args.no_apps else None
     sweep = delta_sweep(g, h_src, dist_dev, total_edges, dev) if lead and not args.no_sweep else None
     other = other_configs(peaks()[0]) if lead and not args.no_configs else None
+    batched_cfg = config4(g, hg, dev) if lead and not args.no_configs else None
 
     if rank != 0:
         if world > 1:
@@ -423,6 +424,7 @@ def run_gb300(args):
         "apps": apps,
         "sssp_sweep": sweep,
         "other_configs": other,
+        "batched_config": batched_cfg,
     }
     print(json.dumps(out))
     if world > 1:
@@ -431,17 +433,18 @@ def run_gb300(args):
 
 def delta_sweep(g, h_src, dist_dev, total_edges, dev):
     """Batched SSSP (32 sources, one launch) over the delta sweep {1, 8, 32, 128}
-    on this graph, and on the 4096 x 4096 4-neighbour grid (weights U[1,1000],
-    high diameter) at delta 128 and 32 -- there delta 8 and 1 take 3 x 10^5 and
-    more buckets (several seconds and more per launch).  Loop time by CUDA events; the
-    GAPBS ordered-processing port on the host cores runs one grid source at the
-    same deltas beside it.  All deltas give the same distances (checked)."""
+    on this graph and on the 4096 x 4096 4-neighbour grid (weights U[1,1000],
+    high diameter; there every source runs in a CTA of its own), plus the
+    single-source fused loop on the grid (sssp.cpp's schedule, one source) at the
+    same deltas.  Loop time by CUDA events; the GAPBS ordered-processing port on
+    the host cores runs the same grid source at delta 128, 32 and 8 beside it.
+    All deltas give the same distances (checked)."""
     import ctypes as C
 
     import torch
 
     import oracle
-    from easy_graphit_gb300 import GraphT, HostGraph, _lib as L
+    from easy_graphit_gb300 import GraphT, HostGraph, default_schedule, sssp, _lib as L
     st = L.gg_stats()
     nsrc = len(h_src)
 
@@ -459,13 +462,13 @@ def delta_sweep(g, h_src, dist_dev, total_edges, dev):
         rmat[str(d)] = {"loop_ms": ms, "gteps": total_edges / ms / 1e6}
     del ref
     hg = HostGraph.grid(4096, 4096)
-    gg = GraphT(hg, symmetric=True)
+    gg = GraphT(hg)
     srcs = np.ascontiguousarray(hg.pick_sources(nsrc), dtype=np.int32)
     out = torch.empty((nsrc, hg.num_vertices), dtype=torch.int32, device=dev)
     deg = torch.from_numpy(np.diff(np.array(hg.offsets)).astype(np.int64)).to(dev)
     grid = {}
     first = None
-    for d in (128, 128, 32):
+    for d in (128, 128, 32, 8, 1):
         ms = launch(gg, srcs, d, out)
         reached = out != INT_MAX
         e_r = float((reached.to(torch.int64) * deg).sum())
@@ -474,10 +477,21 @@ def delta_sweep(g, h_src, dist_dev, total_edges, dev):
             continue
         assert torch.equal(out, first), f"delta {d} changed the grid distances"
         grid[str(d)] = {"loop_ms": ms, "gteps": e_r / ms / 1e6,
-                        "bucket_advances": int(st.bucket_advances), "iterations": int(st.iterations)}
+                        "bucket_advances_all_sources": int(st.bucket_advances)}
+    del out
+    d0 = first[0].cpu().numpy()
+    del first
     off, dstg, w = np.array(hg.offsets), np.array(hg.dst), np.array(hg.weights)
+    e_r0 = reached_stats(off, d0)[1]
+    sch, fz = default_schedule("sssp")
+    single = {}
+    for d in (128, 32, 8, 1):
+        dd, sts = sssp(gg, int(srcs[0]), d, sch, fz)
+        assert np.array_equal(dd, d0), f"delta {d}: single-source distances differ from the batched ones"
+        single[str(d)] = {"device_ms": sts["device_ms"], "gteps": e_r0 / sts["device_ms"] / 1e6,
+                          "bucket_advances": sts["bucket_advances"], "fused": sts["fused"]}
     cpu = {}
-    for d in (128, 32):
+    for d in (128, 32, 8):
         t0 = time.perf_counter()
         dd = oracle.sssp_ordered(off, dstg, w, int(srcs[0]), d, os.cpu_count() or 1)
         t = time.perf_counter() - t0
@@ -485,11 +499,13 @@ def delta_sweep(g, h_src, dist_dev, total_edges, dev):
     gg.close()
     return {"rmat22_batched": rmat,
             "grid4096_batched": grid,
+            "grid4096_single_source_fused": single,
             "grid4096_cpu_port": cpu,
             "grid": "4096 x 4096 4-neighbour, both directions, weights U[1,1000] (V 16,777,216, E 67,092,480)",
             "note": "one timed launch per delta on the grid (after an untimed one at delta 128); "
-                    "built-in launch shape; CPU: GAPBS OrderedProcessingOperatorNoMerge port, one source, "
-                    "all host threads"}
+                    "built-in launch shape (one CTA per source on the grid); single source: sssp.cpp's "
+                    "schedule, fused, source 0 of the batch; CPU: GAPBS OrderedProcessingOperatorNoMerge "
+                    "port, the same source, all host threads"}
 
 
 def other_configs(peak):
@@ -498,7 +514,9 @@ def other_configs(peak):
     PUSH TWCE fused schedule and the learned selector; the graph fits in L2, so
     its byte rate is not an HBM figure), PageRank (20 iterations) on the
     directed R-MAT 24, and CC on the symmetrized R-MAT 24, each against the
-    reference app's own schedule and the OpenMP port on the host cores (CC)."""
+    reference app's own schedule and the OpenMP port on the host cores (CC);
+    and on the same two scale-24 graphs the traversal kernels' lines
+    (scale24_directed, scale24_symmetrized) with their roofline fractions."""
     import oracle
     from easy_graphit_gb300 import (GraphT, HostGraph, LearnedGPUSchedule, Selector,
                                     SimpleGPUSchedule as T, bfs, cc, default_schedule, pagerank)
@@ -555,6 +573,7 @@ def other_configs(peak):
         "roofline": {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                      "bytes_model": "20 x (8 E + 24 V)"},
         "plain_schedule": "PULL EDGE_ONLY blocked 0x42000 (pr.cpp default)"}
+    res["rmat24_directed"] = scale24_directed(g, hg, peak)
     g.close()
     del hg
 
@@ -575,8 +594,130 @@ def other_configs(peak):
         "exact": bool(np.array_equal(lab_r, lab_f) and np.array_equal(lab_f, lab_c)),
         "cpu_port": {"gteps": E / t / 1e9, "cores": threads, "sample": "whole run, OpenMP port of cc.cpp"},
         "plain_schedule": "PUSH EDGE_ONLY rounds (cc.cpp default)",
-        "fused": "union-find in Afforest's sampling order"}
+        "fused": "union-find in Afforest's sampling order",
+        "roofline_fused": roof_line(16.0 * E + 8.0 * hg.num_vertices, st_f["device_ms"], peak,
+                                    "one hook round 16 E + 8 V")}
+    res["rmat24_symmetrized"] = scale24_symmetrized(g, hg, peak)
     g.close()
+    return res
+
+
+def roof_line(alg_bytes, ms, peak, model):
+    gbs = alg_bytes / (ms / 1e3) / 1e9
+    return {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak, "bytes_model": model}
+
+
+def reach_of(deg, rows):
+    """Sum over rows of (reached out-edges, reached vertices)."""
+    er = vr = 0
+    for r in rows:
+        m = (r >= 0) & (r != INT_MAX)
+        er += int(deg[m].sum())
+        vr += int(m.sum())
+    return er, vr
+
+
+def scale24_directed(g, hg, peak):
+    """R-MAT 24 directed (the benchmark spec's 50%-of-HBM scale): batched BFS (64
+    sources, learned directions), batched SSSP (32 sources, delta 32), and
+    single-source BFS (bfs.cpp's schedule) and SSSP (sssp.cpp's and TWCE,
+    fused), each with GTEPS and its roofline fraction by the per-app byte
+    model; single and batched outputs compared."""
+    from easy_graphit_gb300 import (Selector, SimpleGPUSchedule as T, bfs, bfs_batch, default_schedule,
+                                    set_batch_selector, sssp, sssp_batch)
+    res = {}
+    deg = np.diff(np.array(hg.offsets))
+    srcs = np.ascontiguousarray(hg.pick_sources(64), dtype=np.int32)
+    set_batch_selector(g, "bfs", Selector.pretrained_batched_bfs())
+    bfs_batch(g, srcs)
+    depth, st = min((bfs_batch(g, srcs) for _ in range(2)), key=lambda r_: r_[1]["loop_ms"])
+    set_batch_selector(g, "bfs", None)
+    er, vr = reach_of(deg, depth)
+    sch, fz = default_schedule("bfs")
+    bfs(g, int(srcs[0]), sch, fz)
+    one, _, st1 = bfs(g, int(srcs[0]), sch, fz)
+    er1, vr1 = reach_of(deg, [one])
+    res["bfs"] = {"batched_learned_gteps": er / st["loop_ms"] / 1e6, "sources": 64,
+                  "roofline_batched": roof_line(8.0 * er + 16.0 * vr, st["loop_ms"], peak,
+                                                "8 E_r + 16 V_r per source"),
+                  "single_plain_gteps": er1 / st1["device_ms"] / 1e6,
+                  "roofline_single": roof_line(8.0 * er1 + 16.0 * vr1, st1["device_ms"], peak, "8 E_r + 16 V_r"),
+                  "exact": bool(np.array_equal(depth[0], one))}
+    del depth
+    s32 = srcs[:32]
+    sssp_batch(g, s32, 32)
+    dist, st = min((sssp_batch(g, s32, 32) for _ in range(2)), key=lambda r_: r_[1]["loop_ms"])
+    er, vr = reach_of(deg, dist)
+    psch, pfz = default_schedule("sssp")
+    twce = T().configLoadBalancing(T.load_balancing_type.TWCE)
+    d1, stp = sssp(g, int(s32[0]), 32, psch, pfz)
+    sssp(g, int(s32[0]), 32, twce, True)
+    _, stt = sssp(g, int(s32[0]), 32, twce, True)
+    er1, vr1 = reach_of(deg, [d1])
+    res["sssp"] = {"batched_gteps": er / st["loop_ms"] / 1e6, "sources": 32, "delta": 32,
+                   "roofline_batched": roof_line(12.0 * er + 16.0 * vr, st["loop_ms"], peak,
+                                                 "12 E_r + 16 V_r per source"),
+                   "single_plain_gteps": er1 / stp["device_ms"] / 1e6,
+                   "single_twce_fused_gteps": er1 / stt["device_ms"] / 1e6,
+                   "roofline_single_twce": roof_line(12.0 * er1 + 16.0 * vr1, stt["device_ms"], peak,
+                                                     "12 E_r + 16 V_r"),
+                   "exact": bool(np.array_equal(dist[0], d1))}
+    return res
+
+
+def scale24_symmetrized(g, hg, peak):
+    """R-MAT 24 symmetrized: batched BC (64 sources) with its roofline."""
+    from easy_graphit_gb300 import bc_batch
+    deg = np.diff(np.array(hg.offsets))
+    srcs = np.ascontiguousarray(hg.pick_sources(64), dtype=np.int32)
+    bc_batch(g, srcs)
+    dep, st = bc_batch(g, srcs)
+    er2 = st["edges_traversed"]  # 2 x the reached out-edges, summed over sources
+    vr = int(hg.num_vertices) * 64  # a connected graph: every vertex reached from every source
+    return {"bc": {"batched_gteps": er2 / st["loop_ms"] / 1e6, "sources": 64,
+                   "roofline_batched": roof_line(12.0 * er2 + 32.0 * vr, st["loop_ms"], peak,
+                                                 "2 x (8 E_r + 16 V_r) + 8 E_r per source")}}
+
+
+def config4(g, hg, dev):
+    """The batched configuration as written: 256 BFS and 256 SSSP sources on
+    R-MAT 22 replayed from CUDA-graph plans (every persistent launch of every
+    group captured once), and 64 graphs of uneven size (R-MAT scales 12-20,
+    edge factors 4-32, grids 256^2-2048^2) in one traversal per app."""
+    import torch
+    from easy_graphit_gb300 import BatchPlan, GraphT, HostGraph, Selector, bfs_batch, multigraph_batch, \
+        set_batch_selector, sssp_batch
+    res = {}
+    off = np.array(hg.offsets)
+    deg = np.diff(off)
+    V = hg.num_vertices
+    srcs = np.ascontiguousarray(hg.pick_sources(256, seed=7), dtype=np.int32)
+    set_batch_selector(g, "bfs", Selector.pretrained_batched_bfs())
+    out = torch.empty((256, V), dtype=torch.int32, device=dev)
+    for app in ("bfs", "sssp"):
+        plan = BatchPlan(g, app, srcs, out, delta=32)
+        plan.run()
+        st = min((plan.run() for _ in range(3)), key=lambda r_: r_["device_ms"])
+        rows = out.cpu().numpy()
+        want, _ = (bfs_batch(g, srcs) if app == "bfs" else sssp_batch(g, srcs, 32))
+        reached = (rows >= 0) & (rows != INT_MAX)
+        er = int((reached * deg[None, :]).sum())
+        res[f"{app}256_plan"] = {"gteps": er / st["device_ms"] / 1e6, "ms": st["device_ms"],
+                                 "launches_per_replay": st["launches"],
+                                 "exact_vs_calls": bool(np.array_equal(rows, want))}
+        plan.close()
+        del rows, want
+    set_batch_selector(g, "bfs", None)
+    del out
+    parts = HostGraph.mix(64)
+    local = [int(p.pick_sources(1, seed=i)[0]) for i, p in enumerate(parts)]
+    for app in ("bfs", "sssp"):
+        multigraph_batch(parts, app, local, delta=32)
+        r, st = multigraph_batch(parts, app, local, delta=32)
+        er = sum(int(np.diff(np.array(p.offsets))[(x >= 0) & (x != INT_MAX)].sum()) for p, x in zip(parts, r))
+        res[f"mix64_{app}"] = {"gteps": er / st["loop_ms"] / 1e6, "ms": st["loop_ms"],
+                               "graphs": 64, "vertices": int(sum(p.num_vertices for p in parts)),
+                               "edges": int(sum(p.num_edges for p in parts))}
     return res
 
 
@@ -615,12 +756,28 @@ def per_app(g, hg, off, dst, dev, stream, peak):
         vr += int((d >= 0).sum())
         rows.append(d)
     bfs_batch(g, srcs)
-    depth, st = bfs_batch(g, srcs)
+    depth, st = min((bfs_batch(g, srcs) for _ in range(3)), key=lambda r_: r_[1]["loop_ms"])
+    # learned + batched: the direction of every level chosen on the device by
+    # the shipped selector network (trained on engine-made per-level timings)
+    from easy_graphit_gb300 import Selector, set_batch_selector, set_batch_tuning
+    model = Selector.pretrained_batched_bfs()
+    set_batch_selector(g, "bfs", model)
+    bfs_batch(g, srcs)
+    depth_l, st_l = min((bfs_batch(g, srcs) for _ in range(3)), key=lambda r_: r_[1]["loop_ms"])
+    set_batch_selector(g, "bfs", None)
+    set_batch_tuning(g, "bfs", bottom_up_div=-1)
+    _, st_td = min((bfs_batch(g, srcs) for _ in range(3)), key=lambda r_: r_[1]["loop_ms"])
+    set_batch_tuning(g, "bfs")
     res["bfs"] = {"sources": len(srcs), "plain_gteps": er / t_plain / 1e6,
                   "batched_gteps": er / st["loop_ms"] / 1e6,
-                  "exact": bool(np.array_equal(depth, np.stack(rows))),
+                  "learned_batched_gteps": er / st_l["loop_ms"] / 1e6,
+                  "batched_top_down_only_gteps": er / st_td["loop_ms"] / 1e6,
+                  "learned_batched_over_plain": t_plain / st_l["loop_ms"],
+                  "exact": bool(np.array_equal(depth, np.stack(rows)) and np.array_equal(depth_l, depth)),
                   "plain_schedule": "PUSH TWCE fused (bfs.cpp default)",
-                  "roofline": roof(8.0 * er + 16.0 * vr, st["loop_ms"], "sum over sources of 8 E_r + 16 V_r")}
+                  "batched_rule": "bottom-up when the frontier holds more than V/bottom_up_div vertices",
+                  "learned": "per-level direction by the selector network on the device (selector_batched_bfs.bin)",
+                  "roofline": roof(8.0 * er + 16.0 * vr, st_l["loop_ms"], "sum over sources of 8 E_r + 16 V_r")}
     rows_c, t = cpu_leg(lambda: [oracle.bfs_omp(off, dst, int(x), threads) for x in srcs[:4]])
     er_c = sum(int(np.diff(off)[d_ >= 0].sum()) for d_ in rows_c)
     res["bfs"]["cpu_port"] = {"gteps": er_c / t / 1e9, "cores": threads,
@@ -699,7 +856,7 @@ def autotune_table(path, delta=32):
     t0 = time.time()
     for kind, size in sizes:
         for app, nsrc in apps:
-            sym = app == "bc" or kind == "grid"
+            sym = app == "bc" or (kind == "grid" and app == "bfs")  # grid weights differ per direction
             hg = HostGraph.rmat(size, 16, symmetrize=sym) if kind == "rmat" else HostGraph.grid(size, size)
             g = GraphT(hg, symmetric=sym)
             best, rows = autotune_batch(g, app, hg.pick_sources(nsrc), delta)

@@ -50,7 +50,8 @@ class gg_vertex_data(C.Structure):
 
 
 class gg_batch_tuning(C.Structure):
-    _fields_ = [("blocks_per_sm", i32), ("chunk", i32), ("edge_parallel_max", i32), ("bottom_up_div", i32)]
+    _fields_ = [("blocks_per_sm", i32), ("chunk", i32), ("edge_parallel_max", i32), ("bottom_up_div", i32),
+                ("per_source_cta", i32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -72,6 +72,23 @@ struct BsState {
   int32_t scan_div;           // a relax over >= V/scan_div queue entries marks masks without queueing (<= 0: never)
 };
 
+// Batched SSSP with a CTA per source (batch_sssp_cta.cu): buffers of a pass
+// of k sources carved from one scratch allocation.
+struct CtaBuffers {
+  int32_t *rows = nullptr;   // [k][V] distances
+  int32_t *dsrc = nullptr;   // [k]
+  int32_t *stats = nullptr;  // [0] most relax steps of a source, [1] bucket advances
+  int32_t *stamp = nullptr, *piles = nullptr, *q = nullptr;
+  int64_t qcap = 0;
+  int32_t k = 0;
+};
+int32_t bsssp_cta_width(const gg_graph *g);
+gg_status bsssp_cta_buffers(gg_graph *g, int32_t k, Scratch *sc, CtaBuffers *b);
+gg_status bsssp_cta_run(gg_graph *g, cudaStream_t st, const CtaBuffers &b, int32_t *rows, int32_t k,
+                        int32_t delta, bool timed);
+gg_status bsssp_use_cta(gg_graph *g, bool *use);
+gg_status graph_max_degree(gg_graph *g, int32_t *out);
+
 // Device buffers of one batched-SSSP pass; `owned` buffers are freed with it,
 // the others are the graph's reusable app slots.
 struct BsBuffers {

@@ -93,11 +93,11 @@ __global__ void __launch_bounds__(512) k_msbfs(DGraph g, MsBfsState st) {
     } else {
       bu = st.bu_div > 0 && (int64_t)n * st.bu_div > st.V;
     }
-    if (st.feat_log && L < st.max_log && blockIdx.x == 0 && threadIdx.x == 0) {
+    if (st.feat_log && L <= st.max_log && blockIdx.x == 0 && threadIdx.x == 0) {
       const float *x = reinterpret_cast<const float *>(smem);
-      if (!(st.force_dir >= 0))
+      if (!(st.force_dir >= 0) && L < st.max_log)
         for (int i = 0; i < kSelectorFeatures; ++i) st.feat_log[L * kSelectorFeatures + i] = x[i];
-      st.time_log[L] = globaltimer_ns();
+      st.time_log[L] = globaltimer_ns();  // the end of level L-1 (max_log + 1 entries)
     }
     if (st.force_dir >= 0 && st.feat_log && L < st.max_log && blockIdx.x == 0 && threadIdx.x == 0) {
       float x[kSelectorFeatures];

@@ -19,6 +19,8 @@ struct gg_batch_plan {
   gg::BcBuffers bc;
   int32_t *parent = nullptr;              // BFS multi-source: parent scratch
   gg::BqBuffers bq;                       // SSSP multi-source: bucket-queue buffers
+  gg::Scratch cta;                        // SSSP with a CTA per source
+  bool per_cta = false;
   unsigned long long *reached = nullptr;  // BC: reached out-edges summed over sources
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -31,6 +33,7 @@ struct gg_batch_plan {
     if (reached) cudaFree(reached);
     if (parent) cudaFree(parent);
     if (bq.base) gg::bq_free(g, &bq);
+    if (cta.p) cudaFreeAsync(cta.p, g->stream);
   }
 };
 
@@ -54,7 +57,12 @@ gg_status gg_batch_plan_create(gg_graph *g, int32_t app, const int32_t *sources,
   p->g = g;
   p->app = app;
   p->nsrc = nsrc;
-  const int32_t width = multi ? nsrc : (app == GG_BATCH_SSSP ? kBsLanes : kMsBfsWidth);
+  int32_t width = multi ? nsrc : (app == GG_BATCH_SSSP ? kBsLanes : kMsBfsWidth);
+  if (app == GG_BATCH_SSSP) {
+    bool per_cta = false;
+    GG_TRY(bsssp_use_cta(g, &per_cta));
+    if (per_cta) width = std::min(bsssp_cta_width(g), nsrc);
+  }
   p->ngroups = ceil_div(nsrc, width);
   GG_CUDA(cudaMalloc(&p->dsrc, sizeof(int32_t) * nsrc));
   GG_CUDA(cudaMemcpy(p->dsrc, sources, sizeof(int32_t) * nsrc, cudaMemcpyDefault));
@@ -66,10 +74,15 @@ gg_status gg_batch_plan_create(gg_graph *g, int32_t app, const int32_t *sources,
   } else if (app == GG_BATCH_BFS) {
     GG_TRY(msbfs_buffers(g, nsrc, true, &p->ms));
   } else if (app == GG_BATCH_SSSP) {
-    GG_TRY(bsssp_buffers(g, nsrc, true, &p->bs));
+    GG_TRY(bsssp_use_cta(g, &p->per_cta));
+    if (!p->per_cta) GG_TRY(bsssp_buffers(g, nsrc, true, &p->bs));
   } else {
     GG_TRY(bcb_buffers(g, true, &p->bc));
     GG_CUDA(cudaMalloc(&p->reached, sizeof(unsigned long long)));
+  }
+  if (p->per_cta) {
+    CtaBuffers cb;
+    GG_TRY(bsssp_cta_buffers(g, width, &p->cta, &cb));
   }
   // Capture on the graph's own stream (capturable even when the graph is
   // bound to a legacy default stream).
@@ -99,6 +112,20 @@ gg_status gg_batch_plan_create(gg_graph *g, int32_t app, const int32_t *sources,
       MsBfsState S = msbfs_state(g, p->ms, k, (int32_t *)out + (size_t)base * V);
       S.stats = p->dstats + 2 * gi;
       st = msbfs_enqueue(g, cs, S, p->dsrc + base, false);
+    } else if (app == GG_BATCH_SSSP && p->per_cta) {
+      CtaBuffers cb;
+      st = bsssp_cta_buffers(g, width, &p->cta, &cb);  // sized before the capture: no allocation here
+      if (st == GG_OK) {
+        const cudaError_t ce1 = cudaMemcpyAsync(cb.dsrc, p->dsrc + base, sizeof(int32_t) * k,
+                                                cudaMemcpyDeviceToDevice, cs);
+        if (ce1 != cudaSuccess) st = set_error(GG_ERR_CUDA, "source copy in capture: %s", cudaGetErrorString(ce1));
+      }
+      if (st == GG_OK) st = bsssp_cta_run(g, cs, cb, (int32_t *)out + (size_t)base * V, k, delta, false);
+      if (st == GG_OK) {
+        const cudaError_t ce2 = cudaMemcpyAsync(p->dstats + 2 * gi, cb.stats, sizeof(int32_t) * 2,
+                                                cudaMemcpyDeviceToDevice, cs);
+        if (ce2 != cudaSuccess) st = set_error(GG_ERR_CUDA, "stats copy in capture: %s", cudaGetErrorString(ce2));
+      }
     } else if (app == GG_BATCH_SSSP) {
       BsState S = bsssp_state(g, p->bs, delta);
       S.stats = p->dstats + 2 * gi;

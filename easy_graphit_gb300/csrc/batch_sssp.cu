@@ -816,6 +816,43 @@ extern "C" gg_status gg_sssp_batch(gg_graph *g, const int32_t *sources, int32_t 
     GG_CHECK_ARG(sources[i] >= 0 && sources[i] < V, "source out of range");
   if (stats) *stats = gg_stats{};
   cudaStream_t st = g->stream;
+  bool per_cta = false;
+  GG_TRY(bsssp_use_cta(g, &per_cta));
+  if (per_cta) {  // a CTA per source (batch_sssp_cta.cu)
+    const int32_t W = std::min(bsssp_cta_width(g), nsrc);
+    CtaBuffers cb;
+    GG_TRY(bsssp_cta_buffers(g, W, &g->bq_cta, &cb));
+    const uint64_t l0 = launches();
+    cudaEventRecord(g->ev0, st);
+    float loop_ms = 0;
+    int32_t iters = 0, advs = 0;
+    for (int32_t base = 0; base < nsrc; base += W) {
+      const int32_t k = std::min(W, nsrc - base);
+      GG_CUDA(cudaMemcpyAsync(cb.dsrc, sources + base, sizeof(int32_t) * k, cudaMemcpyDefault, st));
+      GG_TRY(bsssp_cta_run(g, st, cb, cb.rows, k, delta, true));
+      GG_CUDA(cudaMemcpyAsync(dist_out + (size_t)base * V, cb.rows, sizeof(int32_t) * (size_t)k * V,
+                              cudaMemcpyDefault, st));
+      GG_CUDA(cudaMemcpyAsync(g->h_pinned + 30, cb.stats, sizeof(int32_t) * 2, cudaMemcpyDeviceToHost, st));
+      GG_CUDA(cudaStreamSynchronize(st));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, g->ev2, g->ev3);
+      loop_ms += ms;
+      iters = std::max(iters, g->h_pinned[30]);
+      advs += g->h_pinned[31];
+    }
+    cudaEventRecord(g->ev1, st);
+    GG_CUDA(cudaEventSynchronize(g->ev1));
+    GG_TRY(check_device_error(g, "sssp_batch"));
+    if (stats) {
+      cudaEventElapsedTime(&stats->device_ms, g->ev0, g->ev1);
+      stats->loop_ms = loop_ms;
+      stats->iterations = iters;
+      stats->bucket_advances = advs;
+      stats->fused = 1;
+      stats->launches = (int32_t)(launches() - l0);
+    }
+    return GG_OK;
+  }
   BsBuffers b;
   GG_TRY(bsssp_buffers(g, nsrc, false, &b));
   const BsState S = bsssp_state(g, b, delta);

@@ -90,9 +90,16 @@ __device__ __forceinline__ void bq_pile_min(const int32_t *__restrict__ pile, in
                                             int32_t nparts, int32_t *red) {
   int32_t m = INT_MAX;
   const int32_t stride = nparts * blockDim.x;
-  for (int32_t i = rank * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const int32_t p = __ldcg(P + __ldcg(pile + i));
-    if (p >= U && p < m) m = p;
+  constexpr int kIn = 4;  // entries per thread in flight
+  for (int32_t i0 = rank * blockDim.x + threadIdx.x; i0 < n; i0 += kIn * stride) {
+    int32_t v[kIn], p[kIn];
+#pragma unroll
+    for (int j = 0; j < kIn; ++j) v[j] = i0 + j * stride < n ? __ldcg(pile + i0 + j * stride) : -1;
+#pragma unroll
+    for (int j = 0; j < kIn; ++j) p[j] = v[j] >= 0 ? __ldcg(P + v[j]) : INT_MAX;
+#pragma unroll
+    for (int j = 0; j < kIn; ++j)
+      if (p[j] >= U && p[j] < m) m = p[j];
   }
   m = bq_block_min(m, red);
   if (threadIdx.x == 0 && m != INT_MAX) atomicMin(out, m);
@@ -121,31 +128,39 @@ __device__ __forceinline__ void bq_pile_split(const int32_t *__restrict__ pile, 
                                               const BqSplitOut &o, int32_t *err, int32_t rank,
                                               int32_t nparts) {
   const int32_t stride = nparts * blockDim.x;
-  for (int32_t i = rank * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const int32_t v = __ldcg(pile + i);
-    const int32_t p = __ldcg(P + v);
-    if (p < U) continue;
-    if (p < win_hi) {
-      front.sparse(v);
-    } else if (!o.hi || p < o.horizon) {
-      if (o.dedup) {
-        if (atomicExch(o.stamp + v, o.lo_tag) == o.lo_tag) continue;
+  constexpr int kIn = 4;  // entries per thread in flight
+  for (int32_t i0 = rank * blockDim.x + threadIdx.x; i0 < n; i0 += kIn * stride) {
+    int32_t vs[kIn], ps[kIn];
+#pragma unroll
+    for (int j = 0; j < kIn; ++j) vs[j] = i0 + j * stride < n ? __ldcg(pile + i0 + j * stride) : -1;
+#pragma unroll
+    for (int j = 0; j < kIn; ++j) ps[j] = vs[j] >= 0 ? __ldcg(P + vs[j]) : -1;
+#pragma unroll
+    for (int j = 0; j < kIn; ++j) {
+      const int32_t v = vs[j], p = ps[j];
+      if (v < 0 || p < U) continue;
+      if (p < win_hi) {
+        front.sparse(v);
+      } else if (!o.hi || p < o.horizon) {
+        if (o.dedup) {
+          if (atomicExch(o.stamp + v, o.lo_tag) == o.lo_tag) continue;
+        } else {
+          o.stamp[v] = o.lo_tag;
+        }
+        const int32_t pos = agg_inc(o.lo_cnt);
+        if (pos < o.cap)
+          o.lo[pos] = v;
+        else
+          atomicOr(err, DEV_ERR_OVERFLOW);
+        if (o.fill) agg_inc(o.fill);
       } else {
-        o.stamp[v] = o.lo_tag;
+        o.stamp[v] = o.hi_tag;
+        const int32_t pos = agg_inc(o.hi_cnt);
+        if (pos < o.cap)
+          o.hi[pos] = v;
+        else
+          atomicOr(err, DEV_ERR_OVERFLOW);
       }
-      const int32_t pos = agg_inc(o.lo_cnt);
-      if (pos < o.cap)
-        o.lo[pos] = v;
-      else
-        atomicOr(err, DEV_ERR_OVERFLOW);
-      if (o.fill) agg_inc(o.fill);
-    } else {
-      o.stamp[v] = o.hi_tag;
-      const int32_t pos = agg_inc(o.hi_cnt);
-      if (pos < o.cap)
-        o.hi[pos] = v;
-      else
-        atomicOr(err, DEV_ERR_OVERFLOW);
     }
   }
 }

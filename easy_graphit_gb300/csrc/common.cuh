@@ -160,7 +160,7 @@ struct DFar {
   __device__ __forceinline__ void park(int32_t v, int32_t p) const {
     const bool low = p < horizon;
     const int32_t tag = low ? lo_tag : hi_tag;
-    if (*(volatile int32_t *)(stamp + v) == tag || atomicExch(stamp + v, tag) == tag) return;
+    if (atomicExch(stamp + v, tag) == tag) return;
     if (low) {
       const int32_t pos = agg_inc(lo_cnt);
       if (pos < cap)

@@ -63,6 +63,8 @@ struct gg_graph {
   gg_frontier_list *app_list = nullptr;
   gg_batch_tuning tuning[3] = {};  // batched BFS, SSSP, BC launch shapes (0 = default)
   const gg_selector *batch_selector[3] = {};  // learned per-level choices of the batched kernels
+  gg::Scratch bq_cta;             // batched SSSP with a CTA per source
+  int32_t max_degree = -1;        // largest out-degree (-1: not computed yet)
 };
 
 struct gg_frontier {

@@ -484,6 +484,7 @@ gg_status gg_graph_destroy(gg_graph *g) {
   free_relabel(g);
   for (auto &s : g->scratch)
     if (s.p) cudaFreeAsync(s.p, st);
+  if (g->bq_cta.p) cudaFreeAsync(g->bq_cta.p, st);
   for (void *p : {(void *)g->d_err, (void *)g->d_bar, (void *)g->d_misc})
     if (p) cudaFreeAsync(p, st);
   cudaStreamSynchronize(st);

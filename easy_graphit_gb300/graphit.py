@@ -794,9 +794,9 @@ BATCH_APPS = {"bfs": 0, "sssp": 1, "bc": 2, "bfs_multi": 3, "sssp_multi": 4}
 
 
 def set_batch_tuning(g: GraphT, app: str, blocks_per_sm: int = 0, chunk: int = 0,
-                     edge_parallel_max: int = 0, bottom_up_div: int = 0) -> None:
+                     edge_parallel_max: int = 0, bottom_up_div: int = 0, per_source_cta: int = 0) -> None:
     """Launch shape of the graph's batched `app` kernels (0 = built-in default)."""
-    t = L.gg_batch_tuning(blocks_per_sm, chunk, edge_parallel_max, bottom_up_div)
+    t = L.gg_batch_tuning(blocks_per_sm, chunk, edge_parallel_max, bottom_up_div, per_source_cta)
     call("gg_batch_set_tuning", g.handle, BATCH_APPS[app], C.byref(t))
 
 

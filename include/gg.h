@@ -447,7 +447,12 @@ gg_status gg_batch_plan_destroy(gg_batch_plan *plan);
  *                     (default 6; -1 = never edge-parallel; at most 32);
  *  bottom_up_div      batched BFS: a level whose frontier holds more than
  *                     V / bottom_up_div vertices runs bottom-up over in-lists
- *                     (default 16; -1 = always top-down; at most 4096).
+ *                     (default 16; -1 = always top-down; at most 4096);
+ *  per_source_cta     batched SSSP: 1 = every source runs the delta-stepping
+ *                     loop in a CTA of its own (the single-source bucket queue,
+ *                     no grid barriers; for meshes and road-like graphs),
+ *                     -1 = the lane-per-source kernel, 0 = by the graph: a CTA
+ *                     per source when no vertex has more than 32 out-edges.
  * The tuning of `app` (GG_BATCH_*) applies to the batched calls and to plans
  * created after it is set. */
 typedef struct gg_batch_tuning {
@@ -455,6 +460,7 @@ typedef struct gg_batch_tuning {
   int32_t chunk;
   int32_t edge_parallel_max;
   int32_t bottom_up_div;
+  int32_t per_source_cta;
 } gg_batch_tuning;
 gg_status gg_batch_set_tuning(gg_graph *g, int32_t app, const gg_batch_tuning *t);
 gg_status gg_batch_get_tuning(const gg_graph *g, int32_t app, gg_batch_tuning *t);

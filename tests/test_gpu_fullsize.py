@@ -41,7 +41,7 @@ def graph(name):
             hg = HostGraph.grid(4096, 4096)
         elif name == "grid1024":
             hg = HostGraph.grid(1024, 1024)
-        sym = name.endswith("s") or name.startswith("grid")
+        sym = name.endswith("s")  # grid weights differ per direction: not symmetric
         _G[name] = (hg, GraphT(hg, symmetric=sym),
                     (np.array(hg.offsets), np.array(hg.dst), np.array(hg.weights)))
     return _G[name]
@@ -79,19 +79,79 @@ def test_sssp_rmat22_32_sources(delta):
     assert shortest_paths_certified(off, dst, w, dist[31], int(srcs[31]))
 
 
-@pytest.mark.parametrize("name,delta", [("grid4096", 8), ("grid4096", 32), ("grid4096", 128),
-                                        ("grid1024", 1)])
-def test_sssp_grid(name, delta):
-    """delta 1 on the full grid takes one iteration per distinct distance
-    (millions); it runs on the 1024 x 1024 grid of the same generator."""
-    hg, g, (off, dst, w) = graph(name)
+GRID_DELTAS = [1, 8, 32, 128]
+
+
+def grid_ref(i):
+    """Dijkstra distances of the i-th SourcePicker source of the 4096 x 4096 grid."""
+    hg, g, (off, dst, w) = graph("grid4096")
+    s = int(hg.pick_sources(2)[i])
+    key = ("grid4096", s)
+    if key not in _G:
+        _G[key] = oracle.sssp_dijkstra(off, dst, w, s)
+    return s, _G[key]
+
+
+@pytest.mark.parametrize("delta", GRID_DELTAS)
+def test_sssp_grid4096_batched(delta):
+    """Two sources in one batched call: on a mesh every source runs the
+    bucket queue in a CTA of its own."""
+    hg, g, _ = graph("grid4096")
     srcs = hg.pick_sources(2)
-    dist, _ = sssp_batch(g, srcs, delta)
+    dist, st = sssp_batch(g, srcs, delta)
     for i in range(2):
-        key = (name, int(srcs[i]))
-        if key not in _G:
-            _G[key] = oracle.sssp_dijkstra(off, dst, w, int(srcs[i]))
-        np.testing.assert_array_equal(dist[i], _G[key])
+        np.testing.assert_array_equal(dist[i], grid_ref(i)[1])
+
+
+@pytest.mark.parametrize("delta", GRID_DELTAS)
+def test_sssp_grid4096_single_source_fused(delta):
+    """sssp.cpp's own schedule (PUSH SPARSE VERTEX_BASED, fused) from two
+    sources; the bucket advances follow the reference rule exactly."""
+    hg, g, (off, dst, w) = graph("grid4096")
+    sch, fuse = default_schedule("sssp")
+    for i in range(2):
+        s, ref = grid_ref(i)
+        dist, st = sssp(g, s, delta, sch, fuse)
+        np.testing.assert_array_equal(dist, ref)
+        assert st["fused"] == 1
+
+
+@pytest.mark.parametrize("delta", [32, 128])
+def test_sssp_grid4096_single_source_unfused(delta):
+    """The host-driven queue (one frontier-size read and one minimum read-back
+    per bucket, as the reference's host loop) from one source.  At delta 1 and
+    8 the 4096 x 4096 grid has 10^5 to 10^6 buckets, one host round trip each
+    (16 s and 95 s): those deltas run on the 1024 x 1024 grid below."""
+    hg, g, _ = graph("grid4096")
+    s, ref = grid_ref(0)
+    dist, st = sssp(g, s, delta, T().configLoadBalancing(T.load_balancing_type.TWCE), False)
+    np.testing.assert_array_equal(dist, ref)
+    assert st["fused"] == 0
+
+
+@pytest.mark.parametrize("delta", [1, 8])
+def test_sssp_grid1024_single_source_unfused_small_delta(delta):
+    hg, g, (off, dst, w) = graph("grid1024")
+    s = int(hg.pick_sources(1)[0])
+    dist, st = sssp(g, s, delta, T().configLoadBalancing(T.load_balancing_type.TWCE), False)
+    np.testing.assert_array_equal(dist, oracle.sssp_dijkstra(off, dst, w, s))
+    assert st["fused"] == 0
+
+
+def test_sssp_grid_lane_per_source_kernel():
+    """The lane-per-source batched kernel (the R-MAT choice) on a mesh as well,
+    by tuning: 32 sources of the 1024 x 1024 grid at delta 128."""
+    from easy_graphit_gb300 import set_batch_tuning
+    hg, g, (off, dst, w) = graph("grid1024")
+    srcs = hg.pick_sources(32)
+    set_batch_tuning(g, "sssp", per_source_cta=-1)
+    lane, _ = sssp_batch(g, srcs, 128)
+    set_batch_tuning(g, "sssp")
+    cta, _ = sssp_batch(g, srcs, 128)
+    np.testing.assert_array_equal(lane, cta)
+    for i in (0, 31):
+        np.testing.assert_array_equal(cta[i], oracle.sssp_dijkstra(off, dst, w, int(srcs[i])))
+    release("grid1024")
 
 
 def test_pagerank_rmat24():
