@@ -392,8 +392,8 @@ gg_status gg_selector_collect(gg_graph *g, int32_t app, int32_t src, int32_t del
  * sized for at most 1,048,576 vertices (about 8 MiB, held on every GPU that
  * loads the library until the process exits); larger graphs are rejected with
  * GG_ERR_INVALID.  The first call on a device (and the first after the calling
- * thread's current context changes) looks up that array's address, so make
- * that call before any stream capture begins.  All calls share the array:
+ * thread's current context changes) looks up that array's address with
+ * cudaGetSymbolAddress, which allocates nothing.  All calls share the array:
  * calls that overlap on the GPU race and must be serialised by the caller.
  * Runs on `stream` (NULL = legacy default stream), reads its status word back
  * and synchronises `stream` before it returns, with the result in depth_out. */
