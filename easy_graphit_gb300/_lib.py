@@ -122,6 +122,7 @@ SIGNATURES: dict[str, tuple] = {
     "gg_frontier_list_insert": (i32, [P, P]),
     "gg_frontier_list_retrieve": (i32, [P, P]),
     "gg_bfs": (i32, [P, C.POINTER(gg_app_schedule), i32, P, P, C.POINTER(gg_stats)]),
+    "gg_bfs_collect_directions": (i32, [P, i32, i32, P, P, C.POINTER(i32)]),
     "gg_sssp": (i32, [P, C.POINTER(gg_app_schedule), i32, i32, P, C.POINTER(gg_stats)]),
     "gg_pagerank": (i32, [P, C.POINTER(gg_app_schedule), i32, f32, P, C.POINTER(gg_stats)]),
     "gg_cc": (i32, [P, C.POINTER(gg_app_schedule), P, C.POINTER(gg_stats)]),

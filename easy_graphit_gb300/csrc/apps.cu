@@ -213,6 +213,29 @@ gg_status seed_sources(gg_graph *g, gg_frontier *f, bool sssp, const VData &vd, 
   return GG_OK;
 }
 
+// A fused BFS whose levels change direction (fused_bfs_do): a hybrid schedule
+// of one push schedule the fused loop supports and one pull schedule (the
+// rule), or a learned schedule with a network (its direction head; s1 pushes).
+static bool bfs_do_plan(const gg_app_schedule *s, BfsDoPlan *p) {
+  if (s->kind == GG_SCHED_HYBRID) {
+    const bool p1 = s->s1.direction == GG_PULL, p2 = s->s2.direction == GG_PULL;
+    if (p1 == p2) return false;
+    p->push = p1 ? &s->s2 : &s->s1;
+    if (!fused_supported(p->push) || p->push->cta_size > kBfsDoMaxCta) return false;
+    p->mode = DO_RULE;
+    p->threshold = s->threshold;
+    p->small_pull = p1;
+    return true;
+  }
+  if (s->kind == GG_SCHED_LEARNED && s->selector && fused_supported(&s->s1) && s->s1.cta_size <= kBfsDoMaxCta) {
+    p->push = &s->s1;
+    p->mode = DO_SELECTOR;
+    p->sel = s->selector;
+    return true;
+  }
+  return false;
+}
+
 gg_status run_bfs(gg_graph *g, const gg_app_schedule *s, const int32_t *srcs, int32_t nsrc,
                   int32_t *parent, int32_t *depth, gg_stats *st) {
   const int32_t V = g->csr.V;
@@ -239,6 +262,18 @@ gg_status run_bfs(gg_graph *g, const gg_app_schedule *s, const int32_t *srcs, in
       }
       return check_device_error(g, "bfs");
     }
+  }
+  BfsDoPlan dp;
+  if (s->fuse && bfs_do_plan(s, &dp)) {
+    int32_t iters = 0, pulls = 0;
+    GG_TRY(fused_bfs_do(g, dp, nsrc, vd, f, &iters, &pulls));
+    if (st) {
+      st->iterations = iters;
+      st->pull_iterations = pulls;
+      st->push_iterations = iters - pulls;
+      st->fused = 1;
+    }
+    return check_device_error(g, "bfs");
   }
   LoopTimer lt(g);
   int32_t n = 1;
@@ -329,6 +364,75 @@ gg_status gg_bfs(gg_graph *g, const gg_app_schedule *s, int32_t src, int32_t *de
   if (parent_out) GG_CUDA(cudaMemcpyAsync(parent_out, parent, sizeof(int32_t) * V, cudaMemcpyDefault, g->stream));
   GG_TRY(reach_stats(g, depth, st));
   GG_CUDA(cudaStreamSynchronize(g->stream));
+  return GG_OK;
+}
+
+// Training data of the fused direction-optimising BFS: the traversal from src
+// with every level pushed (bfs.cpp's PUSH TWCE schedule), then with every
+// level pulled, twice each.  A level's result does not depend on its
+// direction, so level l starts from the same state in every run.
+gg_status gg_bfs_collect_directions(gg_graph *g, int32_t src, int32_t max_rows, float *feats,
+                                    float *times, int32_t *nrows) {
+  GG_CHECK_ARG(g && feats && times && nrows && max_rows > 0, "bad arguments");
+  GG_CHECK_ARG(src >= 0 && src < g->csr.V, "source out of range");
+  const int32_t V = g->csr.V;
+  *nrows = 0;
+  int32_t *parent = nullptr, *depth = nullptr;
+  GG_TRY(app_array(g, 0, V, &parent));
+  GG_TRY(app_array(g, 1, V, &depth));
+  gg_frontier *f = nullptr;
+  GG_TRY(app_frontier(g, &f));
+  gg_schedule push;
+  gg_schedule_init(&push);
+  push.load_balancing = GG_LB_TWCE;
+  cudaStream_t st = g->stream;
+  float *dfeat = nullptr;
+  unsigned long long *dtime = nullptr;
+  GG_CUDA(dev_alloc(&dfeat, sizeof(float) * kSelectorFeatures * (size_t)max_rows, st));
+  GG_CUDA(dev_alloc(&dtime, sizeof(unsigned long long) * ((size_t)max_rows + 1), st));
+  std::vector<float> best(2 * (size_t)max_rows, INFINITY);
+  std::vector<unsigned long long> ht((size_t)max_rows + 1);
+  int32_t levels = -1;
+  gg_status status = GG_OK;
+  for (int rep = 0; rep < 4 && status == GG_OK; ++rep) {
+    const int dir = rep & 1;
+    VData vd{};
+    vd.parent = parent;
+    vd.depth = depth;
+    vd.src = src;
+    BfsDoPlan p;
+    p.push = &push;
+    p.mode = dir ? DO_FORCE_PULL : DO_FORCE_PUSH;
+    p.feat_log = dfeat;
+    p.time_log = dtime;
+    p.max_log = max_rows;
+    int32_t lv = 0, pulls = 0;
+    if ((status = vertexset_apply_impl(g, nullptr, GG_VUDF_BFS_RESET, vd)) != GG_OK ||
+        (status = frontier_set_single(f, src)) != GG_OK ||
+        (status = fused_bfs_do(g, p, 1, vd, f, &lv, &pulls)) != GG_OK ||
+        (status = check_device_error(g, "bfs_collect_directions")) != GG_OK)
+      break;
+    if (levels >= 0 && lv != levels) {
+      status = set_error(GG_ERR_STATE, "level counts differ between direction runs (%d, %d)", levels, lv);
+      break;
+    }
+    levels = lv;
+    const int32_t rows = std::min(levels, max_rows);
+    if (cudaMemcpy(ht.data(), dtime, sizeof(unsigned long long) * ((size_t)rows + 1), cudaMemcpyDeviceToHost) !=
+            cudaSuccess ||
+        (rep == 0 && cudaMemcpy(feats, dfeat, sizeof(float) * kSelectorFeatures * (size_t)rows,
+                                cudaMemcpyDeviceToHost) != cudaSuccess)) {
+      status = set_error(GG_ERR_CUDA, "reading the direction timings failed");
+      break;
+    }
+    for (int32_t l = 0; l < rows; ++l)
+      best[2 * l + dir] = std::min(best[2 * l + dir], (float)((double)(ht[l + 1] - ht[l]) * 1e-6));
+  }
+  cudaFreeAsync(dfeat, st);
+  cudaFreeAsync(dtime, st);
+  GG_TRY(status);
+  *nrows = std::min(levels, max_rows);
+  for (int32_t i = 0; i < 2 * *nrows; ++i) times[i] = best[i];
   return GG_OK;
 }
 

@@ -147,27 +147,6 @@ gg_status msbfs_buffers(gg_graph *g, int32_t nsrc, bool owned, MsBfsBuffers *b);
 MsBfsState msbfs_state(gg_graph *g, const MsBfsBuffers &b, int32_t k, int32_t *depth_rows);
 gg_status msbfs_enqueue(gg_graph *g, cudaStream_t st, const MsBfsState &S, const int32_t *dsrc,
                         bool timed);
-// Features of one level of a batched BFS from its frontier statistics (the
-// same 12 as the single-source selector's, selector_data.cu make_features).
-__device__ __forceinline__ void msbfs_features(float *x, double n, double sd, double sd2, double mx, double vis_v,
-                                               double vis_e, int32_t level, double V, double E) {
-  E = E > 1 ? E : 1;
-  const double mean = n > 0 ? sd / n : 0.0;
-  const double var = n > 0 ? fmax(0.0, sd2 / n - mean * mean) : 0.0;
-  x[0] = (float)(log2(1 + n) / 32);
-  x[1] = (float)(log2(1 + sd) / 32);
-  x[2] = (float)(log2(1 + fmax(0.0, V - vis_v)) / 32);
-  x[3] = (float)(log2(1 + fmax(0.0, E - vis_e)) / 32);
-  x[4] = (float)(log2(1 + mean) / 16);
-  x[5] = (float)(log2(1 + mx) / 32);
-  x[6] = (float)(log2(1 + var) / 64);
-  x[7] = (float)(min(level, 256) / 256.0);
-  x[8] = (float)(log2(V) / 32);
-  x[9] = (float)(log2(1 + E) / 32);
-  x[10] = (float)(n / V);
-  x[11] = (float)(sd / E);
-}
-
 // ------------------------------------------------------------ batched BC
 // Device buffers of one batched-BC pass (64 sources); `owned` buffers are
 // freed with it, the others are the graph's reusable app slots.

@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(512) k_msbfs(DGraph g, MsBfsState st) {
     } else if (st.sel || st.feat_log) {
       float *x = reinterpret_cast<float *>(smem);  // scratch until the level's TWCE bins
       if (threadIdx.x == 0)
-        msbfs_features(x, (double)n, sd, sd2, mx, vis_v, vis_e, L, (double)st.V, (double)st.E);
+        selector_features(x, (double)n, sd, sd2, mx, vis_v, vis_e, L, (double)st.V, (double)st.E);
       __syncthreads();
       bu = st.sel ? selector_pull(st.sel, x, x + 16) : (st.bu_div > 0 && (int64_t)n * st.bu_div > st.V);
     } else {
@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(512) k_msbfs(DGraph g, MsBfsState st) {
     }
     if (st.force_dir >= 0 && st.feat_log && L < st.max_log && blockIdx.x == 0 && threadIdx.x == 0) {
       float x[kSelectorFeatures];
-      msbfs_features(x, (double)n, sd, sd2, mx, vis_v, vis_e, L, (double)st.V, (double)st.E);
+      selector_features(x, (double)n, sd, sd2, mx, vis_v, vis_e, L, (double)st.V, (double)st.E);
       for (int i = 0; i < kSelectorFeatures; ++i) st.feat_log[L * kSelectorFeatures + i] = x[i];
     }
     vis_v = fmin((double)st.V, vis_v + n);

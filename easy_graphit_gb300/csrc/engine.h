@@ -213,6 +213,26 @@ gg_status fused_multi_enqueue(gg_graph *g, cudaStream_t st, bool sssp, const int
                               const int32_t **stats);
 gg_status fused_bfs(gg_graph *g, const gg_schedule *s, int32_t n0, const VData &vd,
                     gg_frontier *f, int32_t *iters, bool *ran);
+// Direction-optimising fused BFS (fused.cu k_bfs_do): each level pushes with
+// `push` (a fused-supported LB) or pulls over the in-lists, as `mode` decides
+// on the device -- the hybrid rule (pull when the frontier is small iff
+// small_pull; small = n <= threshold * V), the selector's direction head, or a
+// forced direction.  Optional logs: features of level l (feat_log[l][12]) and
+// the start time of each level plus the end time (time_log, max_log + 1).
+enum : int32_t { DO_RULE = 0, DO_SELECTOR = 1, DO_FORCE_PUSH = 2, DO_FORCE_PULL = 3 };
+constexpr int kBfsDoMaxCta = 512;  // the loop is compiled for CTAs of at most 512 threads, 3 per SM
+struct BfsDoPlan {
+  const gg_schedule *push = nullptr;
+  int32_t mode = DO_RULE;
+  float threshold = 0.f;
+  int32_t small_pull = 0;
+  const gg_selector *sel = nullptr;
+  float *feat_log = nullptr;
+  unsigned long long *time_log = nullptr;
+  int32_t max_log = 0;
+};
+gg_status fused_bfs_do(gg_graph *g, const BfsDoPlan &p, int32_t n0, const VData &vd, gg_frontier *f,
+                       int32_t *iters, int32_t *pulls);
 gg_status fused_sssp(gg_graph *g, const gg_schedule *s, int32_t n0, int32_t delta, const VData &vd,
                      gg_pq *pq, int32_t *iters, int64_t *advances, bool *ran);
 // Bucket-queue buffers for V vertices (pool memory on the graph's stream), their

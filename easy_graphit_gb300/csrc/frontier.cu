@@ -565,11 +565,20 @@ gg_status gg_frontier_destroy(gg_frontier *f) {
   if (f->owned_by_pq)
     return set_error(GG_ERR_STATE, "the frontier belongs to a priority queue; gg_pq_destroy releases it");
   cudaStream_t st = f->g->stream;
+  cudaError_t e = cudaSuccess;
   for (void *p : {(void *)f->q_in, (void *)f->q_out, (void *)f->cnt, (void *)f->bm_in,
                   (void *)f->bm_out, (void *)f->by_in, (void *)f->by_out, (void *)f->dedup})
-    if (p) cudaFreeAsync(p, st);
-  cudaStreamSynchronize(st);
+    if (p) {
+      const cudaError_t r = cudaFreeAsync(p, st);
+      if (e == cudaSuccess) e = r;
+    }
+  const cudaError_t r = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = r;
   delete f;
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // reported here, not by the next call's launch check
+    return set_error(GG_ERR_CUDA, "releasing the frontier failed: %s", cudaGetErrorString(e));
+  }
   return GG_OK;
 }
 

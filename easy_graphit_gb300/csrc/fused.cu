@@ -13,6 +13,7 @@
 #include "bucket_queue.cuh"
 #include "engine.h"
 #include "lb.cuh"
+#include "selector.h"
 #include "udf.cuh"
 
 namespace gg {
@@ -295,6 +296,224 @@ gg_status fused_bfs(gg_graph *g, const gg_schedule *s, int32_t n0, const VData &
   }
   GG_TRY(read_stats(g, iters, nullptr));
   *ran = true;
+  return GG_OK;
+}
+
+// ------------------------------------------- direction-optimising BFS loop
+// The fused BFS loop with a direction per level, decided on the device at the
+// top of the level by every CTA alike (the same statistics in, the same answer
+// out): the HybridGPUSchedule rule "s1 while |frontier| <= t*V, else s2"
+// (operators.cpp:516-532) when s1 / s2 are one push and one pull schedule, the
+// selector network's direction head, or a forced direction (training data).
+//
+// Frontiers are always the sparse queue.  A push level runs the push schedule's
+// LB function over it; a pull level walks every vertex still without a parent
+// with an 8-lane group over its in-list and stops at the first in-neighbour
+// whose depth is the previous level (depth doubles as the frontier bitmap of
+// bfs.cpp's PULL BITMAP schedule; the vertex's own group is the only writer of
+// its parent and depth, so no atomics).  Both directions append the vertices
+// they reach to the next queue and add their out-degrees to the statistics of
+// that frontier (sum, sum of squares, maximum), which the next level's rule or
+// network reads: nothing returns to the host between levels.
+
+struct DoArgs {
+  DGraph t;                    // in-lists: the transpose, or the CSR itself on a symmetric graph
+  unsigned long long *lstat;   // [3][4] frontier statistics per level (rotating)
+  const float *sel;            // network parameters (DO_SELECTOR)
+  int32_t mode;
+  float threshold;             // DO_RULE: small frontier <=> n <= threshold * V
+  int32_t small_pull;          // DO_RULE: the small-frontier schedule is the pull one
+  float *feat_log;             // optional: features of level l (training data)
+  unsigned long long *time_log;  // optional: start time of level l, end time last
+  int32_t max_log;
+};
+
+struct DoKernelArgs {
+  FusedArgs a;
+  DoArgs d;
+};
+
+// bfs.cpp's UDF (UBfs) that also adds the out-degree of each vertex it reaches
+// to the CTA's statistics of the next frontier.
+struct UBfsNote {
+  static constexpr bool kWeight = false;
+  int32_t *parent, *depth;
+  const int32_t *off;
+  unsigned long long *s_stat;  // shared memory [3]
+  int32_t level;
+  __device__ __forceinline__ bool filter(int32_t v) const { return vload(parent + v) == -1; }
+  __device__ __forceinline__ bool apply(int32_t s, int32_t d, int32_t) const {
+    if (!cas(parent + d, -1, s)) return false;
+    depth[d] = level;
+    const unsigned long long k = (unsigned long long)(__ldg(off + d + 1) - __ldg(off + d));
+    atomicAdd(s_stat, k);
+    atomicAdd(s_stat + 1, k * k);
+    atomicMax(s_stat + 2, k);
+    return true;
+  }
+};
+
+template <int LB>
+__global__ void __launch_bounds__(kBfsDoMaxCta, 3) k_bfs_do(DoKernelArgs ka) {
+  extern __shared__ int4 smem[];
+  __shared__ unsigned long long s_stat[3];
+  __shared__ float s_x[kSelIn + 2 * kSelHidden];
+  __shared__ double s_vis[2];  // vertices and out-edges of the frontiers so far (thread 0's; the same in every CTA)
+  __shared__ int32_t s_pulls;
+  const FusedArgs &a = ka.a;
+  const DoArgs &d = ka.d;
+  if (threadIdx.x == 0) {
+    s_vis[0] = s_vis[1] = 0.0;
+    s_pulls = 0;
+  }
+  int32_t level = 1;
+  LoopClock clk;
+  clk.start(a.loop_limit_ns);
+  for (;; ++level) {
+    const int32_t n = *(volatile int32_t *)(a.cnt3 + (level - 1) % 3);
+    if (n == 0 || stopped(a.stop, a.err)) break;
+    const bool logged = d.feat_log && level - 1 <= d.max_log;
+    if (threadIdx.x == 0) {
+      const volatile unsigned long long *ls = d.lstat + 4 * ((level - 1) % 3);
+      const double sd = (double)ls[0];
+      if (d.mode == DO_SELECTOR || logged)
+        selector_features(s_x, (double)n, sd, (double)ls[1], (double)ls[2], s_vis[0], s_vis[1], level - 1,
+                          (double)a.g.V, (double)a.g.E);
+      s_vis[0] = fmin((double)a.g.V, s_vis[0] + n);
+      s_vis[1] = fmin((double)a.g.E, s_vis[1] + sd);
+      s_stat[0] = s_stat[1] = s_stat[2] = 0ull;
+      if (blockIdx.x == 0) {
+        a.cnt3[(level + 1) % 3] = 0;
+        for (int i = 0; i < 4; ++i) d.lstat[4 * ((level + 1) % 3) + i] = 0ull;
+      }
+    }
+    __syncthreads();
+    bool pull;
+    if (d.mode == DO_FORCE_PUSH)
+      pull = false;
+    else if (d.mode == DO_FORCE_PULL)
+      pull = true;
+    else if (d.mode == DO_SELECTOR)
+      pull = selector_pull(d.sel, s_x, s_x + kSelIn);
+    else
+      pull = ((float)n <= d.threshold * (float)a.g.V) == (d.small_pull != 0);
+    if (logged && blockIdx.x == 0 && threadIdx.x == 0) {
+      if (level - 1 < d.max_log)
+        for (int i = 0; i < kSelectorFeatures; ++i) d.feat_log[(level - 1) * kSelectorFeatures + i] = s_x[i];
+      d.time_log[level - 1] = globaltimer_ns();
+    }
+    const DOut out = sparse_out(a, (level & 1) ? a.q1 : a.q0, level);
+    if (!pull) {
+      const Enum en{(level & 1) ? a.q0 : a.q1, nullptr, n};
+      const EdgeF<UBfsNote, false> f{UBfsNote{a.vd.parent, a.vd.depth, a.g.off, s_stat, level},
+                                     DIn{IN_ALL, nullptr, nullptr}, DIn{IN_ALL, nullptr, nullptr}, true};
+      run_lb<LB>(a.g, en, n, f, out, smem, blockIdx.x, gridDim.x);
+    } else {
+      if (threadIdx.x == 0) ++s_pulls;
+      const int32_t lane = threadIdx.x & 31, sub = lane & 7, gbase = lane & ~7;
+      const uint32_t gmask = 0xFFu << gbase;
+      const int32_t prev = level - 1;
+      for (int32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; v < a.g.V;
+           v += (gridDim.x * blockDim.x) >> 3) {
+        if (__ldcg(a.vd.parent + v) != -1) continue;
+        const int32_t kb = __ldg(d.t.off + v), ke = __ldg(d.t.off + v + 1);
+        int32_t hit = -1;
+        for (int32_t k0 = kb; k0 < ke; k0 += 8) {
+          int32_t u = -1;
+          if (k0 + sub < ke) {
+            u = __ldg(d.t.dst + k0 + sub);
+            if (__ldcg(a.vd.depth + u) != prev) u = -1;
+          }
+          const uint32_t bits = (__ballot_sync(gmask, u >= 0) >> gbase) & 0xFFu;
+          if (bits) {
+            hit = __shfl_sync(gmask, u, gbase + __ffs(bits) - 1);
+            break;
+          }
+        }
+        if (hit >= 0 && sub == 0) {
+          a.vd.parent[v] = hit;
+          a.vd.depth[v] = level;
+          out.sparse(v);
+          const unsigned long long k = (unsigned long long)(__ldg(a.g.off + v + 1) - __ldg(a.g.off + v));
+          atomicAdd(s_stat, k);
+          atomicAdd(s_stat + 1, k * k);
+          atomicMax(s_stat + 2, k);
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && (s_stat[0] | s_stat[2])) {
+      unsigned long long *nx = d.lstat + 4 * (level % 3);
+      atomicAdd(nx, s_stat[0]);
+      atomicAdd(nx + 1, s_stat[1]);
+      atomicMax(nx + 2, s_stat[2]);
+    }
+    clk.tick(a.stop);
+    if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.stats[0] = level - 1;
+    a.stats[1] = s_pulls;
+    if (d.time_log && level - 1 <= d.max_log) d.time_log[level - 1] = globaltimer_ns();
+  }
+}
+
+// Statistics of the first frontier (the n0 sources on the queue); the other
+// two slots cleared.
+__global__ void k_bfs_do_seed(const int32_t *__restrict__ q, int32_t n0, const int32_t *__restrict__ off,
+                              unsigned long long *lstat) {
+  __shared__ unsigned long long s[3];
+  if (threadIdx.x < 3) s[threadIdx.x] = 0ull;
+  __syncthreads();
+  for (int32_t i = threadIdx.x; i < n0; i += blockDim.x) {
+    const int32_t v = q[i];
+    const unsigned long long k = (unsigned long long)(off[v + 1] - off[v]);
+    atomicAdd(s, k);
+    atomicAdd(s + 1, k * k);
+    atomicMax(s + 2, k);
+  }
+  __syncthreads();
+  if (threadIdx.x < 12) lstat[threadIdx.x] = threadIdx.x < 3 ? s[threadIdx.x] : 0ull;
+}
+
+gg_status fused_bfs_do(gg_graph *g, const BfsDoPlan &p, int32_t n0, const VData &vd, gg_frontier *f,
+                       int32_t *iters, int32_t *pulls) {
+  const gg_schedule *s = p.push;
+  if (!s || !fused_supported(s) || s->cta_size > kBfsDoMaxCta)
+    return set_error(GG_ERR_UNSUPPORTED, "push schedule cannot be fused (or CTA size above %d)", kBfsDoMaxCta);
+  GG_CHECK_ARG(vd.parent && vd.depth, "the direction-optimising loop needs parent and depth");
+  GG_CHECK_ARG(p.mode != DO_SELECTOR || p.sel, "no selector");
+  GG_TRY(ensure_transpose(g));
+  const GraphStore *t = g->csc ? g->csc.get() : &g->csr;
+  void *ls = nullptr;
+  GG_TRY(scratch_get_app(g, 7, sizeof(unsigned long long) * 12, &ls));
+  GG_TRY(init_counts(g, n0));
+  note_launch();
+  k_bfs_do_seed<<<1, 256, 0, g->stream>>>(f->q_in, n0, g->csr.off, static_cast<unsigned long long *>(ls));
+  GG_CUDA(cudaGetLastError());
+  DoKernelArgs ka{};
+  ka.a = make_args(g, f, vd);
+  ka.d.t = t->view();
+  ka.d.t.nbuckets = 0;
+  ka.d.lstat = static_cast<unsigned long long *>(ls);
+  ka.d.sel = p.mode == DO_SELECTOR ? selector_params(p.sel) : nullptr;
+  ka.d.mode = p.mode;
+  ka.d.threshold = p.threshold;
+  ka.d.small_pull = p.small_pull;
+  ka.d.feat_log = p.feat_log;
+  ka.d.time_log = p.time_log;
+  ka.d.max_log = p.max_log;
+  const int cta = s->cta_size;
+  const size_t sm = lb_smem(s->load_balancing, cta);
+  switch (s->load_balancing) {
+    case GG_LB_VERTEX_BASED: GG_TRY(coop_launch(g, k_bfs_do<GG_LB_VERTEX_BASED>, cta, sm, ka)); break;
+    case GG_LB_WM: GG_TRY(coop_launch(g, k_bfs_do<GG_LB_WM>, cta, sm, ka)); break;
+    case GG_LB_TWCE: GG_TRY(coop_launch(g, k_bfs_do<GG_LB_TWCE>, cta, sm, ka)); break;
+    default: GG_TRY(coop_launch(g, k_bfs_do<GG_LB_CM>, cta, sm, ka)); break;
+  }
+  int64_t np = 0;
+  GG_TRY(read_stats(g, iters, &np));
+  *pulls = (int32_t)np;
   return GG_OK;
 }
 

@@ -495,6 +495,9 @@ gg_status gg_graph_destroy(gg_graph *g) {
   if (g->ev3) cudaEventDestroy(g->ev3);
   if (g->own_stream) cudaStreamDestroy(g->own_stream);
   delete g;
+  // Any failure above is reported here rather than by the next call's launch check.
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(GG_ERR_CUDA, "releasing the graph failed: %s", cudaGetErrorString(e));
   return GG_OK;
 }
 

@@ -43,12 +43,35 @@ constexpr int kSelW1 = 0, kSelB1 = kSelW1 + kSelIn * kSelHidden, kSelW2 = kSelB1
               kSelB2 = kSelW2 + kSelHidden * kSelHidden, kSelW3 = kSelB2 + kSelHidden,
               kSelB3 = kSelW3 + kSelHidden * kSelOut;
 
+// The 12 selector features of one frontier (make_features of selector_data.cu,
+// on the device): frontier size n, its out-degree sum sd, sum of squares sd2
+// and maximum mx, the vertices and edges visited before it, and its level.
+__device__ __forceinline__ void selector_features(float *x, double n, double sd, double sd2, double mx,
+                                                  double vis_v, double vis_e, int32_t level, double V,
+                                                  double E) {
+  E = E > 1 ? E : 1;
+  const double mean = n > 0 ? sd / n : 0.0;
+  const double var = n > 0 ? fmax(0.0, sd2 / n - mean * mean) : 0.0;
+  x[0] = (float)(log2(1 + n) / 32);
+  x[1] = (float)(log2(1 + sd) / 32);
+  x[2] = (float)(log2(1 + fmax(0.0, V - vis_v)) / 32);
+  x[3] = (float)(log2(1 + fmax(0.0, E - vis_e)) / 32);
+  x[4] = (float)(log2(1 + mean) / 16);
+  x[5] = (float)(log2(1 + mx) / 32);
+  x[6] = (float)(log2(1 + var) / 64);
+  x[7] = (float)(min(level, 256) / 256.0);
+  x[8] = (float)(log2(V) / 32);
+  x[9] = (float)(log2(1 + E) / 32);
+  x[10] = (float)(n / V);
+  x[11] = (float)(sd / E);
+}
+
 // Direction head of the network on one feature vector x (12 floats), computed
 // by the calling CTA inside a persistent kernel: fp32 accumulation over
 // bf16-rounded operands, as the tensor-core forward pass computes it.  h is
 // 2*64 floats of shared memory.  Every thread of the CTA calls it and gets the
 // same answer: true when the network picks PULL.
-__device__ __forceinline__ bool selector_pull(const float *__restrict__ p, const float *x, float *h) {
+static __device__ __noinline__ bool selector_pull(const float *__restrict__ p, const float *x, float *h) {
   auto bf = [](float v) { return __bfloat162float(__float2bfloat16_rn(v)); };
   const int j = threadIdx.x;
   if (j < kSelHidden) {

@@ -10,6 +10,7 @@ libgg.so on the GPU; this module only marshals arguments.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from enum import IntEnum
 from pathlib import Path
 from typing import Optional
@@ -165,7 +166,12 @@ D, LB, FC, PR_ = (SimpleGPUSchedule.direction_type, SimpleGPUSchedule.load_balan
 
 class LearnedGPUSchedule:
     """Per-iteration schedule from the learned selector; `fallback` (the
-    hand-written GraphIt schedule) is used when no selector is attached."""
+    hand-written GraphIt schedule) is used when no selector is attached.
+    Unfused, each iteration's (direction, load balancing, frontier) comes from
+    the network on the host.  Fused (BFS): one persistent loop pushes with the
+    fallback's load balancing or pulls, level by level, as the network's
+    direction head decides on the device (Selector.pretrained_fused_bfs() is
+    trained for that loop)."""
 
     def __init__(self, selector: "Selector", fallback: SimpleGPUSchedule | None = None):
         self.selector = selector
@@ -181,7 +187,6 @@ def app_schedule(s, fuse: bool = False) -> L.gg_app_schedule:
         a.s1 = s.fallback.to_c()
         a.s2 = s.fallback.to_c()
         a.selector = s.selector._h if s.selector is not None else None
-        a.fuse = 0
         return a
     if isinstance(s, HybridGPUSchedule):
         a.kind = 1
@@ -379,6 +384,7 @@ class GraphT:
              1 if symmetric else 0, C.byref(h))
         self._h = h
         self._keep = None
+        self._deps = weakref.WeakSet()  # frontiers, queues, lists and plans made on this graph
         self.num_vertices, self.num_edges, self.symmetric = V, E, symmetric
 
     @property
@@ -399,8 +405,18 @@ class GraphT:
     def sync(self) -> None:
         call("gg_graph_sync", self._h)
 
+    def _adopt(self, obj) -> None:
+        self._deps.add(obj)
+
     def close(self) -> None:
+        """Releases the graph and, first, every object still open on it (their
+        device memory is tied to the graph's)."""
         if getattr(self, "_h", None):
+            for d in list(getattr(self, "_deps", ())):
+                try:
+                    d.close()
+                except Exception:
+                    pass
             lib().gg_graph_destroy(self._h)
             self._h = None
 
@@ -432,12 +448,14 @@ class VertexSubset:
         call("gg_frontier_create", g.handle, int(init_all), C.byref(h))
         self._h = h
         self._owned = True
+        g._adopt(self)
 
     @classmethod
     def _view(cls, g: GraphT, handle) -> "VertexSubset":
         """A frontier owned by someone else (a priority queue's)."""
         v = cls.__new__(cls)
         v.g, v._h, v._owned = g, handle, False
+        g._adopt(v)
         return v
 
     @property
@@ -479,12 +497,15 @@ class VertexSubset:
         call("gg_frontier_read", self._h, _ptr(out), n.value, C.byref(n))
         return out
 
+    def close(self) -> None:
+        # a view of a priority queue's frontier is released with the queue
+        if getattr(self, "_h", None) and getattr(self, "_owned", True):
+            lib().gg_frontier_destroy(self._h)
+        self._h = None
+
     def __del__(self):
         try:
-            # a view of a priority queue's frontier is released with the queue
-            if getattr(self, "_h", None) and getattr(self, "_owned", True):
-                lib().gg_frontier_destroy(self._h)
-            self._h = None
+            self.close()
         except Exception:
             pass
 
@@ -621,6 +642,7 @@ class PriorityQueue:
         h = C.c_void_p()
         call("gg_pq_create", g.handle, _ptr(priorities), init_priority, delta, src, C.byref(h))
         self._h = h
+        g._adopt(self)
 
     @property
     def handle(self):
@@ -655,6 +677,7 @@ class VertexFrontierList:
         h = C.c_void_p()
         call("gg_frontier_list_create", g.handle, C.byref(h))
         self._h = h
+        g._adopt(self)
 
     def insert(self, f: "VertexSubset") -> None:
         call("gg_frontier_list_insert", self._h, f.handle)
@@ -772,6 +795,7 @@ class BatchPlan:
         call("gg_batch_plan_create", g.handle, BATCH_APPS[app], _np_ptr(srcs), len(srcs),
              delta, _ptr(out), C.byref(h))
         self._h = h
+        g._adopt(self)
 
     def run(self) -> dict:
         st = L.gg_stats()
@@ -817,6 +841,18 @@ def collect_batched_directions(g: GraphT, sources, max_rows: int = 1024):
     n = C.c_int32()
     call("gg_batch_collect", g.handle, BATCH_APPS["bfs"], _np_ptr(srcs), len(srcs), max_rows,
          _np_ptr(feats), _np_ptr(times), C.byref(n))
+    return feats[:n.value].copy(), times[:n.value].copy()
+
+
+def collect_fused_directions(g: GraphT, src: int, max_rows: int = 8192):
+    """Per-level features [levels, 12] and times [levels, 2] (ms; push, pull)
+    of the fused direction-optimising BFS from src (every level forced each
+    way, best of two runs)."""
+    feats = np.empty((max_rows, N_FEATURES), dtype=np.float32)
+    times = np.empty((max_rows, 2), dtype=np.float32)
+    n = C.c_int32()
+    call("gg_bfs_collect_directions", g.handle, int(src), max_rows, _np_ptr(feats), _np_ptr(times),
+         C.byref(n))
     return feats[:n.value].copy(), times[:n.value].copy()
 
 
@@ -928,6 +964,14 @@ class Selector:
         (selector_batched_bfs.bin, trained by `easy_graphit_gb300.selector_train
         --batched-bfs`; manifest selector_batched_bfs.json)."""
         return cls.load(str(Path(__file__).resolve().parent / "selector_batched_bfs.bin"))
+
+    @classmethod
+    def pretrained_fused_bfs(cls) -> "Selector":
+        """The per-level direction model of the fused single-source BFS loop
+        shipped with the package (selector_fused_bfs.bin, trained by
+        `easy_graphit_gb300.selector_train --fused-bfs`; manifest
+        selector_fused_bfs.json)."""
+        return cls.load(str(Path(__file__).resolve().parent / "selector_fused_bfs.bin"))
 
     def save(self, path: str) -> None:
         call("gg_selector_save", self._h, str(path).encode())

@@ -2,6 +2,7 @@
 
     python -m easy_graphit_gb300.selector_train [--out easy_graphit_gb300/selector_model.bin]
     python -m easy_graphit_gb300.selector_train --batched-bfs [--out .../selector_batched_bfs.bin]
+    python -m easy_graphit_gb300.selector_train --fused-bfs [--out .../selector_fused_bfs.bin]
 
 --batched-bfs trains the per-level direction of the batched BFS instead: on
 each training graph, 64 sources are traversed with every level top-down and
@@ -10,6 +11,11 @@ levels where the two differ more weigh more (the row is repeated).  The model
 runs on the device inside the batched kernel (gg_batch_set_selector); held-out
 seeds compare it with both fixed directions, the built-in rule and the
 per-level optimum.
+
+--fused-bfs does the same for the fused single-source BFS loop (gg_bfs with
+fuse = 1 and a learned schedule): every training source is traversed with every
+level pushed and then pulled (gg_bfs_collect_directions); held-out graphs
+compare the network with bfs.cpp's two schedules and with its hybrid rule fused.
 
 Training graphs: R-MAT at scales 18 to 24 with skew a in [0.45, 0.75] (b = c =
 (0.95 - a) / 2) and 2-D grids, GAPBS-seeded; for each, BFS and SSSP runs
@@ -31,12 +37,14 @@ from pathlib import Path
 import numpy as np
 
 from .graphit import (GraphT, HostGraph, LearnedGPUSchedule, Selector, bfs, bfs_batch, cc,
-                      collect_batched_directions, collect_timings, default_schedule, labels_from_times,
+                      collect_batched_directions, collect_fused_directions, collect_timings, default_schedule,
+                      labels_from_times,
                       set_batch_selector, set_batch_tuning, sssp)
 
 PKG = Path(__file__).resolve().parent
 DEFAULT_OUT = PKG / "selector_model.bin"
 BATCHED_BFS_OUT = PKG / "selector_batched_bfs.bin"
+FUSED_BFS_OUT = PKG / "selector_fused_bfs.bin"
 
 TRAIN_SEEDS = [101, 102, 103]
 HELDOUT_SEEDS = [901, 902]
@@ -226,8 +234,124 @@ def main_batched_bfs(a, log):
     log(json.dumps(manifest))
 
 
+# ------------------------------------------------- fused single-source BFS
+def collect_fused_bfs(scales, skews, grids, log):
+    X, T = [], []
+    for name, scale, a, seed in training_graphs(scales, skews):
+        for sym in (True, False):
+            hg = rmat(scale, a, seed, sym)
+            g = GraphT(hg, symmetric=sym)
+            deg = np.diff(np.array(hg.offsets))
+            srcs = [int(np.argmax(deg))] + [int(v) for v in hg.pick_sources(3, seed=seed + 5)]
+            for src in srcs:
+                f, t = collect_fused_directions(g, src)
+                X.append(f)
+                T.append(t)
+            log(f"{name}{' sym' if sym else ''}: {sum(len(x) for x in X[-4:])} levels from 4 sources")
+            g.close()
+    for n in grids:
+        hg = HostGraph.grid(n, n, seed=TRAIN_SEEDS[0])
+        g = GraphT(hg, symmetric=True)
+        for src in hg.pick_sources(2, seed=7):
+            f, t = collect_fused_directions(g, int(src))
+            X.append(f)
+            T.append(t)
+        log(f"grid{n}: {sum(len(x) for x in X[-2:])} levels from 2 sources")
+        g.close()
+    return np.concatenate(X), np.concatenate(T)
+
+
+def fused_heldout_graphs():
+    return (("rmat16_sym", HostGraph.rmat(16, 16, symmetrize=True), True),
+            ("rmat20_sym", rmat(20, 0.57, HELDOUT_SEEDS[0], True), True),
+            ("rmat22", rmat(22, 0.57, HELDOUT_SEEDS[1], False), False),
+            ("rmat21_a0.65_sym", rmat(21, 0.65, HELDOUT_SEEDS[1], True), True),
+            ("grid1024", HostGraph.grid(1024, 1024, seed=HELDOUT_SEEDS[0]), True))
+
+
+def evaluate_fused(model, log, reps=5):
+    """Held-out graphs, two sources each (the highest-degree vertex and a
+    SourcePicker source): per-level cost of each policy on the measured level
+    times, and whole runs (best of `reps` trial times) of bfs.cpp's two
+    schedules -- PUSH TWCE fused, and the hybrid "power" schedule unfused as
+    the reference runs it -- against the same hybrid rule fused and the
+    network fused; depths compared."""
+    rows = []
+    plain, plain_fuse = default_schedule("bfs")
+    power, _ = default_schedule("bfs", power=True)
+    learned = LearnedGPUSchedule(model)
+    for name, hg, sym in fused_heldout_graphs():
+        g = GraphT(hg, symmetric=sym)
+        deg = np.diff(np.array(hg.offsets))
+        for src in (int(np.argmax(deg)), int(hg.pick_sources(1, seed=HELDOUT_SEEDS[0])[0])):
+            f, t = collect_fused_directions(g, src)
+            pull = model.predict(f)[:, 0]
+            per_level = {"push_ms": float(t[:, 0].sum()), "pull_ms": float(t[:, 1].sum()),
+                         "learned_ms": float(t[np.arange(len(t)), pull].sum()),
+                         "optimum_ms": float(t.min(1).sum())}
+
+            def run(sched, fuse):
+                best, out = None, None
+                for _ in range(reps):
+                    out, _, st = bfs(g, src, sched, fuse)
+                    best = st["device_ms"] if best is None else min(best, st["device_ms"])
+                return best, out
+            runs = {}
+            outs = []
+            for label, sched, fuse in (("plain_push_twce_fused", plain, plain_fuse),
+                                       ("power_hybrid_unfused", power, False),
+                                       ("power_hybrid_fused", power, True),
+                                       ("learned_fused", learned, True)):
+                runs[label], d = run(sched, fuse)
+                outs.append(d)
+            if not all(np.array_equal(outs[0], d) for d in outs[1:]):
+                raise AssertionError(f"{name}: depths differ between schedules")
+            row = {"graph": name, "V": hg.num_vertices, "E": hg.num_edges, "source": src, "levels": int(len(t)),
+                   "per_level_cost": per_level, "runs_ms": runs}
+            rows.append(row)
+            log(json.dumps(row))
+        g.close()
+    return rows
+
+
+def main_fused_bfs(a, log):
+    scales = [int(s) for s in a.scales.split(",")]
+    skews = [float(s) for s in a.skews.split(",")]
+    grids = [int(s) for s in a.grids.split(",") if s]
+    t0 = time.time()
+    X, T = collect_fused_bfs(scales, skews, grids, log)
+    Xr, lab = batched_rows(X, T)
+    log(f"collected {len(X)} levels ({len(Xr)} weighted rows) in {time.time() - t0:.1f}s")
+    model = Selector(seed=27491095)
+    loss = model.train(Xr, lab, epochs=a.epochs, lr=a.lr)
+    pull = model.predict(X)[:, 0]
+    acc = float((pull == (T[:, 1] < T[:, 0])).mean())
+    regret = float(T[np.arange(len(T)), pull].sum() / T.min(1).sum())
+    log(f"loss {loss:.4f} direction accuracy {acc:.3f} time / per-level optimum {regret:.3f}")
+    out = a.out if a.out != str(DEFAULT_OUT) else str(FUSED_BFS_OUT)
+    model.save(out)
+    evals = evaluate_fused(model, log)
+    manifest = {
+        "file": Path(out).name, "params": int(len(model.params)),
+        "architecture": "12 -> 64 -> 64 -> 11 (bf16 MLP); the direction head picks each level's direction "
+                        "(push or pull) inside the fused single-source BFS loop, on the device; the other "
+                        "heads are unused",
+        "training": {"levels": int(len(X)), "weighted_rows": int(len(Xr)), "scales": scales, "skews": skews,
+                     "grids": grids, "seeds": TRAIN_SEEDS,
+                     "sources_per_graph": "4 (R-MAT: the highest-degree vertex and 3 SourcePicker sources), "
+                                          "2 (grids)",
+                     "epochs": a.epochs, "lr": a.lr, "final_loss": loss, "direction_accuracy": acc,
+                     "time_over_per_level_optimum": regret},
+        "heldout": evals,
+    }
+    Path(out).with_suffix(".json").write_text(json.dumps(manifest, indent=1))
+    log(json.dumps(manifest))
+
+
 def main():
     p = argparse.ArgumentParser()
+    p.add_argument("--fused-bfs", action="store_true",
+                   help="train the per-level direction of the fused single-source BFS (selector_fused_bfs.bin)")
     p.add_argument("--batched-bfs", action="store_true",
                    help="train the per-level direction of the batched BFS (selector_batched_bfs.bin)")
     p.add_argument("--out", default=str(DEFAULT_OUT))
@@ -242,6 +366,9 @@ def main():
     log = lambda m: print(m, flush=True)
     if a.batched_bfs:
         main_batched_bfs(a, log)
+        return
+    if a.fused_bfs:
+        main_fused_bfs(a, log)
         return
     scales = [int(s) for s in a.scales.split(",")]
     skews = [float(s) for s in a.skews.split(",")]

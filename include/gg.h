@@ -178,6 +178,8 @@ enum { GG_GRAPH_SYMMETRIC = 1 };
 gg_status gg_graph_create(const int32_t *offsets, const int32_t *dst,
                           const int32_t *weights, int32_t num_vertices,
                           int64_t num_edges, uint32_t flags, gg_graph **out);
+/* Frontiers, priority queues, frontier lists and batch plans made on g hold
+ * pointers into it: destroy them before the graph. */
 gg_status gg_graph_destroy(gg_graph *g);
 gg_status gg_graph_info(const gg_graph *g, int32_t *num_vertices,
                         int64_t *num_edges);
@@ -325,9 +327,24 @@ uint64_t gg_kernel_launches(void);
 gg_status gg_memory_trim(size_t keep_bytes);
 
 /* BFS from src: depth_out[v] = hop distance (-1 unreached); parent_out (may be
- * NULL) = the parent array of bfs.cpp (parent[src] = src). */
+ * NULL) = the parent array of bfs.cpp (parent[src] = src).
+ * With fuse = 1, a hybrid schedule of one push schedule (VERTEX_BASED, TWCE,
+ * CM or WM, SPARSE creation) and one PULL schedule, or a learned schedule with
+ * a selector, runs as ONE persistent kernel that picks each level's direction
+ * on the device: the hybrid rule of operators.cpp:516-532, or the network's
+ * direction head on the frontier statistics (no host round trip per level;
+ * the reference runs bfs.cpp's hybrid "power" schedule unfused).  Pull levels
+ * scan the in-lists of unvisited vertices, stopping at the first in-neighbour
+ * on the previous level.  Depths are the same whatever the directions;
+ * parents are a valid BFS tree. */
 gg_status gg_bfs(gg_graph *g, const gg_app_schedule *s, int32_t src,
                  int32_t *depth_out, int32_t *parent_out, gg_stats *stats);
+/* Training data of that loop's direction (no reference counterpart): BFS from
+ * src with every level pushed (PUSH TWCE), then every level pulled, twice
+ * each.  feats[l][12] = the selector's features of level l; times[l][2] = its
+ * best time in ms (push, pull); *nrows = levels recorded (at most max_rows). */
+gg_status gg_bfs_collect_directions(gg_graph *g, int32_t src, int32_t max_rows,
+                                    float *feats, float *times, int32_t *nrows);
 /* Delta-stepping SSSP from src: dist_out[v] (INT_MAX unreached). */
 gg_status gg_sssp(gg_graph *g, const gg_app_schedule *s, int32_t src,
                   int32_t delta, int32_t *dist_out, gg_stats *stats);

@@ -1,0 +1,124 @@
+"""The fused direction-optimising BFS loop (gg_bfs with fuse = 1 and a hybrid or
+learned schedule): one persistent kernel whose levels push or pull as the
+hybrid rule (operators.cpp:516-532), the selector's direction head or a forced
+direction decides on the device.  Depths must equal the oracle's whatever the
+directions, and parents must form a valid BFS tree."""
+import numpy as np
+import pytest
+
+import oracle
+from easy_graphit_gb300 import (GraphT, HostGraph, HybridGPUSchedule, LearnedGPUSchedule, Selector, bfs,
+                                collect_fused_directions, default_schedule)
+from easy_graphit_gb300 import SimpleGPUSchedule as T
+from easy_graphit_gb300.graphit import bfs_multi
+
+pytestmark = pytest.mark.gpu
+
+_G = {}
+
+
+def graph(name):
+    if name not in _G:
+        if name == "sym14":
+            hg, sym = HostGraph.rmat(14, 16, symmetrize=True), True
+        elif name == "dir14":
+            hg, sym = HostGraph.rmat(14, 8), False
+        elif name == "grid64":
+            hg, sym = HostGraph.grid(64, 64), True  # unweighted BFS: the in-lists are the out-lists
+        elif name == "chain":
+            n = 3000  # a path: one vertex per level
+            hg, sym = HostGraph.from_edges(n, np.arange(n - 1, dtype=np.int32),
+                                           np.arange(1, n, dtype=np.int32), symmetrize=True), True
+        g = GraphT(hg, symmetric=sym)
+        _G[name] = (hg, g, np.array(hg.offsets), np.array(hg.dst))
+    return _G[name]
+
+
+def power(threshold):
+    """bfs.cpp's "power" schedule (PUSH TWCE while |frontier| <= t*V, else PULL
+    BITMAP VERTEX_BASED), with its threshold."""
+    s, _ = default_schedule("bfs", power=True, threshold=threshold)
+    return s
+
+
+def check(hg, off, dst, src, depth, parent):
+    np.testing.assert_array_equal(depth, oracle.bfs(off, dst, src))
+    assert oracle.bfs_check_parent(off, dst, src, depth, parent) == 0
+
+
+def sources(hg, off, k=2):
+    deg = np.diff(off)
+    return [int(np.argmax(deg))] + [int(s) for s in hg.pick_sources(k)]
+
+
+@pytest.mark.parametrize("name", ["sym14", "dir14", "grid64", "chain"])
+@pytest.mark.parametrize("threshold", [0.0, 0.05, 0.12, 2.0])
+def test_hybrid_fused_matches_oracle(name, threshold):
+    hg, g, off, dst = graph(name)
+    for src in sources(hg, off):
+        depth, parent, st = bfs(g, src, power(threshold), True, with_parent=True)
+        check(hg, off, dst, src, depth, parent)
+        assert st["fused"] == 1
+        assert st["push_iterations"] + st["pull_iterations"] == st["iterations"]
+        if threshold == 0.0:  # no frontier is "small": every level pulls
+            assert st["push_iterations"] == 0
+        if threshold == 2.0:  # every frontier is small: every level pushes
+            assert st["pull_iterations"] == 0
+
+
+@pytest.mark.parametrize("name", ["sym14", "dir14", "grid64"])
+def test_hybrid_fused_equals_hybrid_unfused(name):
+    """The same rule decides the same directions fused and unfused."""
+    hg, g, off, dst = graph(name)
+    src = sources(hg, off)[0]
+    d1, _, s1 = bfs(g, src, power(0.05), True)
+    d2, _, s2 = bfs(g, src, power(0.05), False)
+    np.testing.assert_array_equal(d1, d2)
+    assert (s1["push_iterations"], s1["pull_iterations"]) == (s2["push_iterations"], s2["pull_iterations"])
+
+
+@pytest.mark.parametrize("lb", ["VERTEX_BASED", "CM", "WM"])
+def test_hybrid_fused_other_push_strategies(lb):
+    hg, g, off, dst = graph("sym14")
+    s1 = T().configLoadBalancing(getattr(T.load_balancing_type, lb))
+    s2 = T().configDirection(T.direction_type.PULL, T.pull_frontier_rep_type.BITMAP)
+    src = sources(hg, off)[0]
+    depth, parent, st = bfs(g, src, HybridGPUSchedule(s1, s2).bindThreshold(0.05), True, with_parent=True)
+    check(hg, off, dst, src, depth, parent)
+    assert st["fused"] == 1 and st["pull_iterations"] > 0
+
+
+@pytest.mark.parametrize("name", ["sym14", "dir14", "grid64"])
+@pytest.mark.parametrize("seed", [1, 2])
+def test_learned_fused_any_network_is_exact(name, seed):
+    """Untrained networks pick arbitrary directions; the depths stay exact."""
+    hg, g, off, dst = graph(name)
+    sched = LearnedGPUSchedule(Selector(seed=seed))
+    for src in sources(hg, off):
+        depth, parent, st = bfs(g, src, sched, True, with_parent=True)
+        check(hg, off, dst, src, depth, parent)
+        assert st["fused"] == 1
+
+
+def test_multi_source_hybrid_fused():
+    hg, g, off, dst = graph("sym14")
+    srcs = np.array(hg.pick_sources(5), dtype=np.int32)
+    depth, st = bfs_multi(g, srcs, power(0.05), True)
+    want = np.min(np.stack([np.where(d < 0, np.iinfo(np.int32).max, d)
+                            for d in (oracle.bfs(off, dst, int(s)) for s in srcs)]), 0)
+    want = np.where(want == np.iinfo(np.int32).max, -1, want)
+    np.testing.assert_array_equal(depth, want)
+    assert st["fused"] == 1
+
+
+@pytest.mark.parametrize("name", ["sym14", "dir14", "chain"])
+def test_collect_directions(name):
+    hg, g, off, dst = graph(name)
+    src = sources(hg, off)[0]
+    f, t = collect_fused_directions(g, src)
+    levels = int(oracle.bfs(off, dst, src).max()) + 1  # the last level finds nothing new
+    assert len(f) == len(t) == levels
+    assert np.isfinite(t).all() and (t > 0).all()
+    assert f[0, 0] == pytest.approx(np.log2(2) / 32)  # one source on the first frontier
+    # the first level's frontier is the source; its out-degree is feature 1
+    assert f[0, 1] == pytest.approx(np.log2(1 + np.diff(off)[src]) / 32, rel=1e-6)
