@@ -553,6 +553,7 @@ def other_configs(peak):
         "V": hg.num_vertices, "E": hg.num_edges, "source": "highest degree",
         "plain_gteps": er / st["device_ms"] / 1e6, "learned_gteps": er / st2["device_ms"] / 1e6,
         "exact": ok and bool(np.array_equal(d2, d)),
+        "schedules": bfs_single_lines(g, off, dst, src),
         "cpu_port": {"gteps": er / t / 1e9, "cores": threads, "sample": "OpenMP port of bfs.cpp, mean of 5"},
         "note": "PUSH TWCE fused (bfs.cpp default); graph L2-resident"}
     g.close()
@@ -600,6 +601,42 @@ def other_configs(peak):
     res["rmat24_symmetrized"] = scale24_symmetrized(g, hg, peak)
     g.close()
     return res
+
+
+def bfs_single_lines(g, off, dst, src, reps=5):
+    """One-source BFS under each schedule, best of `reps` device times: bfs.cpp's
+    PUSH TWCE fused and its hybrid "power" schedule unfused (as the reference
+    runs them), the same hybrid rule fused (one persistent kernel, direction
+    per level on the device), and the fused loop with the selector's direction
+    head (selector_fused_bfs.bin).  GTEPS = reached out-edges / time; depths
+    compared across schedules."""
+    from pathlib import Path
+
+    import easy_graphit_gb300 as G
+    plain, pf = G.default_schedule("bfs")
+    power, _ = G.default_schedule("bfs", power=True)
+    runs = [("plain_push_twce_fused", plain, pf), ("power_hybrid_unfused", power, False),
+            ("power_hybrid_fused", power, True)]
+    if (Path(G.__file__).resolve().parent / "selector_fused_bfs.bin").exists():
+        runs.append(("learned_fused", G.LearnedGPUSchedule(G.Selector.pretrained_fused_bfs()), True))
+    out, first = {}, None
+    for name, sch, fz in runs:
+        best = None
+        for _ in range(reps):
+            d, _, st = G.bfs(g, src, sch, fz)
+            if best is None or st["device_ms"] < best[1]["device_ms"]:
+                best = (d, st)
+        d, st = best
+        if first is None:
+            first = d
+        er = int(np.diff(off)[d >= 0].sum())
+        out[name] = {"gteps": er / st["device_ms"] / 1e6, "ms": st["device_ms"],
+                     "pull_levels": st["pull_iterations"], "levels": st["iterations"],
+                     "exact": bool(np.array_equal(d, first))}
+    fixed = max(v["gteps"] for k, v in out.items() if not k.startswith("learned"))
+    if "learned_fused" in out:
+        out["learned_fused_over_best_fixed"] = out["learned_fused"]["gteps"] / fixed
+    return out
 
 
 def roof_line(alg_bytes, ms, peak, model):
@@ -717,7 +754,7 @@ def config4(g, hg, dev):
         er = sum(int(np.diff(np.array(p.offsets))[(x >= 0) & (x != INT_MAX)].sum()) for p, x in zip(parts, r))
         res[f"mix64_{app}"] = {"gteps": er / st["loop_ms"] / 1e6, "ms": st["loop_ms"],
                                "graphs": 64, "vertices": int(sum(p.num_vertices for p in parts)),
-                               "edges": int(sum(p.num_edges for p in parts))}
+                               "edges": int(sum(p.num_edges for p in parts)), "classes": st["classes"]}
     return res
 
 
@@ -782,6 +819,7 @@ def per_app(g, hg, off, dst, dev, stream, peak):
     er_c = sum(int(np.diff(off)[d_ >= 0].sum()) for d_ in rows_c)
     res["bfs"]["cpu_port"] = {"gteps": er_c / t / 1e9, "cores": threads,
                               "sample": "4 of the 64 sources, OpenMP port of bfs.cpp (oracle)"}
+    res["bfs"]["single_source_schedules"] = bfs_single_lines(g, off, dst, int(srcs[0]))
     # BC: bc.cpp's PUSH TWCE fused per source vs 64 sources per launch
     sch, fz = default_schedule("bc")
     t_plain, er2, rows = 0.0, 0, []

@@ -155,6 +155,7 @@ SIGNATURES: dict[str, tuple] = {
     "gg_selector_load": (i32, [C.c_char_p, C.POINTER(P)]),
     "gg_selector_collect": (i32, [P, i32, i32, i32, i32, P, P, P]),
     "gg_sssp_batch": (i32, [P, P, i32, i32, P, C.POINTER(gg_stats)]),
+    "gg_sssp_parts": (i32, [P, P, i32, P, i32, P, C.POINTER(gg_stats)]),
     "gg_batch_set_selector": (i32, [P, i32, P]),
     "gg_batch_collect": (i32, [P, i32, P, i32, i32, P, P, C.POINTER(i32)]),
 }

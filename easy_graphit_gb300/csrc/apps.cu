@@ -167,6 +167,8 @@ void count_dir(gg_stats *st, const gg_schedule *s) {
 
 }  // namespace
 
+gg_status app_reach_stats(gg_graph *g, const int32_t *val, gg_stats *st) { return reach_stats(g, val, st); }
+
 gg_status scratch_get_app(gg_graph *g, int slot, size_t bytes, void **p) {
   Scratch &s = g->app[slot];
   if (s.bytes < bytes) {

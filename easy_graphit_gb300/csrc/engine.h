@@ -138,6 +138,9 @@ gg_status ensure_blocked(gg_graph *g, bool reverse, int32_t block_size, const Gr
 gg_status check_device_error(gg_graph *g, const char *what);
 gg_status scratch_get(gg_graph *g, int slot, size_t bytes, void **p);
 gg_status scratch_get_app(gg_graph *g, int slot, size_t bytes, void **p);
+// stats->vertices_reached / edges_traversed of a result array (reached: >= 0
+// and != INT_MAX).
+gg_status app_reach_stats(gg_graph *g, const int32_t *val, gg_stats *st);
 int resident_grid(const void *kernel, int cta, size_t smem, int sm_count);
 
 // ---- cc_uf.cu
@@ -220,7 +223,7 @@ gg_status fused_bfs(gg_graph *g, const gg_schedule *s, int32_t n0, const VData &
 // forced direction.  Optional logs: features of level l (feat_log[l][12]) and
 // the start time of each level plus the end time (time_log, max_log + 1).
 enum : int32_t { DO_RULE = 0, DO_SELECTOR = 1, DO_FORCE_PUSH = 2, DO_FORCE_PULL = 3 };
-constexpr int kBfsDoMaxCta = 512;  // the loop is compiled for CTAs of at most 512 threads, 3 per SM
+constexpr int kBfsDoMaxCta = 512;  // the loop is compiled for CTAs of at most 512 threads, 4 per SM
 struct BfsDoPlan {
   const gg_schedule *push = nullptr;
   int32_t mode = DO_RULE;

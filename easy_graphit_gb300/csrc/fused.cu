@@ -7,6 +7,8 @@
 // Sparse-queue counts rotate through three slots: iteration L reads slot
 // (L-1)%3, appends to slot L%3 and clears slot (L+1)%3, whose last reader
 // finished before the previous barrier -- one barrier per iteration.
+#include <cooperative_groups/reduce.h>
+
 #include <cstdlib>
 
 #include "bq_loop.cuh"
@@ -212,8 +214,8 @@ gg_status bq_start(const BqBuffers &b, int32_t n0, cudaStream_t st) {
   return GG_OK;
 }
 
-template <class K, class A>
-static gg_status coop_launch(gg_graph *g, K kernel, int cta, size_t smem, A &a) {
+template <class K, class A, class... More>
+static gg_status coop_launch(gg_graph *g, K kernel, int cta, size_t smem, A &a, More &...more) {
   int per_sm = 0;
   if (smem > 48 * 1024)
     GG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -221,7 +223,7 @@ static gg_status coop_launch(gg_graph *g, K kernel, int cta, size_t smem, A &a) 
   if (per_sm < 1) return set_error(GG_ERR_UNSUPPORTED, "fused kernel does not fit on an SM");
   const int grid = per_sm * g->sm_count;
   GG_CUDA(cudaMemsetAsync(g->d_bar, 0, sizeof(uint32_t) * 2, g->stream));
-  void *args[] = {&a};
+  void *args[] = {&a, &more...};
   GG_CUDA(cudaEventRecord(g->ev2, g->stream));
   note_launch();
   GG_CUDA(cudaLaunchCooperativeKernel((const void *)kernel, grid, cta, args, smem, g->stream));
@@ -318,9 +320,11 @@ gg_status fused_bfs(gg_graph *g, const gg_schedule *s, int32_t n0, const VData &
 
 struct DoArgs {
   DGraph t;                    // in-lists: the transpose, or the CSR itself on a symmetric graph
-  unsigned long long *lstat;   // [3][4] frontier statistics per level (rotating)
+  unsigned long long *lstat;   // [3][4] statistics of the frontier of each level (rotating):
+                               // out-degree sum (u64), sum of squares (double), maximum (u64)
   const float *sel;            // network parameters (DO_SELECTOR)
   int32_t mode;
+  int32_t stats;               // gather frontier statistics (the network and the logs read them)
   float threshold;             // DO_RULE: small frontier <=> n <= threshold * V
   int32_t small_pull;          // DO_RULE: the small-frontier schedule is the pull one
   float *feat_log;             // optional: features of level l (training data)
@@ -333,79 +337,116 @@ struct DoKernelArgs {
   DoArgs d;
 };
 
-// bfs.cpp's UDF (UBfs) that also adds the out-degree of each vertex it reaches
-// to the CTA's statistics of the next frontier.
+// A CTA's statistics of the next frontier, in shared memory.
+struct DoStat {
+  unsigned int sum, mx;
+  float sq;
+};
+
+// Adds the out-degree k of a vertex entering the next frontier: one reduction
+// over the threads that reach this point together, one shared atomic each.
+__device__ __forceinline__ void do_note(DoStat *s, uint32_t k) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  const uint32_t sum = cg::reduce(g, k, cg::plus<uint32_t>());
+  const float sq = cg::reduce(g, (float)k * (float)k, cg::plus<float>());
+  const uint32_t mx = cg::reduce(g, k, cg::greater<uint32_t>());
+  if (g.thread_rank() == 0) {
+    atomicAdd(&s->sum, sum);
+    atomicAdd(&s->sq, sq);
+    atomicMax(&s->mx, mx);
+  }
+}
+
+// bfs.cpp's UDF (UBfs) that also notes the out-degree of each vertex it
+// reaches when the loop gathers statistics.
 struct UBfsNote {
   static constexpr bool kWeight = false;
   int32_t *parent, *depth;
   const int32_t *off;
-  unsigned long long *s_stat;  // shared memory [3]
+  DoStat *stat;  // shared memory; null: no statistics
   int32_t level;
   __device__ __forceinline__ bool filter(int32_t v) const { return vload(parent + v) == -1; }
   __device__ __forceinline__ bool apply(int32_t s, int32_t d, int32_t) const {
     if (!cas(parent + d, -1, s)) return false;
     depth[d] = level;
-    const unsigned long long k = (unsigned long long)(__ldg(off + d + 1) - __ldg(off + d));
-    atomicAdd(s_stat, k);
-    atomicAdd(s_stat + 1, k * k);
-    atomicMax(s_stat + 2, k);
+    if (stat) do_note(stat, (uint32_t)(__ldg(off + d + 1) - __ldg(off + d)));
     return true;
   }
 };
 
+// Dynamic shared memory: the push strategy's, then (DO_SELECTOR) the staged
+// network parameters.
+__host__ __device__ __forceinline__ size_t do_lb_smem_aligned(size_t lb_bytes) { return (lb_bytes + 15) & ~size_t(15); }
+
 template <int LB>
-__global__ void __launch_bounds__(kBfsDoMaxCta, 3) k_bfs_do(DoKernelArgs ka) {
+__global__ void __launch_bounds__(kBfsDoMaxCta, 4) k_bfs_do(DoKernelArgs ka, uint32_t lb_bytes) {
   extern __shared__ int4 smem[];
-  __shared__ unsigned long long s_stat[3];
-  __shared__ float s_x[kSelIn + 2 * kSelHidden];
-  __shared__ double s_vis[2];  // vertices and out-edges of the frontiers so far (thread 0's; the same in every CTA)
+  __shared__ DoStat s_stat;
+  __shared__ float s_x[16 + 64];
+  __shared__ int32_t s_pull;
+  __shared__ float s_in[4];    // n, out-degree sum, sum of squares, maximum of this level's frontier
+  __shared__ float s_vis[2];   // vertices and out-edges of the frontiers so far (the same in every CTA)
   __shared__ int32_t s_pulls;
   const FusedArgs &a = ka.a;
   const DoArgs &d = ka.d;
+  float *wsel = reinterpret_cast<float *>(reinterpret_cast<char *>(smem) + do_lb_smem_aligned(lb_bytes));
+  if (d.mode == DO_SELECTOR) selector_stage(d.sel, wsel);
   if (threadIdx.x == 0) {
-    s_vis[0] = s_vis[1] = 0.0;
+    s_vis[0] = s_vis[1] = 0.f;
     s_pulls = 0;
   }
+  __syncthreads();
   int32_t level = 1;
   LoopClock clk;
   clk.start(a.loop_limit_ns);
   for (;; ++level) {
+    // the frontier statistics are loaded together with its size (one round trip)
+    unsigned long long r = 0ull;
+    if (d.stats && threadIdx.x < 3) r = *(volatile unsigned long long *)(d.lstat + 4 * ((level - 1) % 3) + threadIdx.x);
     const int32_t n = *(volatile int32_t *)(a.cnt3 + (level - 1) % 3);
     if (n == 0 || stopped(a.stop, a.err)) break;
     const bool logged = d.feat_log && level - 1 <= d.max_log;
-    if (threadIdx.x == 0) {
-      const volatile unsigned long long *ls = d.lstat + 4 * ((level - 1) % 3);
-      const double sd = (double)ls[0];
-      if (d.mode == DO_SELECTOR || logged)
-        selector_features(s_x, (double)n, sd, (double)ls[1], (double)ls[2], s_vis[0], s_vis[1], level - 1,
-                          (double)a.g.V, (double)a.g.E);
-      s_vis[0] = fmin((double)a.g.V, s_vis[0] + n);
-      s_vis[1] = fmin((double)a.g.E, s_vis[1] + sd);
-      s_stat[0] = s_stat[1] = s_stat[2] = 0ull;
-      if (blockIdx.x == 0) {
-        a.cnt3[(level + 1) % 3] = 0;
-        for (int i = 0; i < 4; ++i) d.lstat[4 * ((level + 1) % 3) + i] = 0ull;
+    // The level's direction, decided by warp 0 alone (statistics, features,
+    // network) and handed to the CTA by one barrier.
+    if (threadIdx.x < 32) {
+      const int32_t l = threadIdx.x;
+      bool pull = d.mode == DO_FORCE_PULL ||
+                  (d.mode == DO_RULE && ((float)n <= d.threshold * (float)a.g.V) == (d.small_pull != 0));
+      if (d.stats) {
+        if (l < 3) s_in[1 + l] = l == 1 ? (float)__longlong_as_double((long long)r) : (float)r;
+        if (l == 0) {
+          s_in[0] = (float)n;
+          s_stat.sum = s_stat.mx = 0u;
+          s_stat.sq = 0.f;
+        }
+        __syncwarp();
+        if (l < kSelectorFeatures && (d.mode == DO_SELECTOR || logged))
+          s_x[l] = selector_feature(l, s_in[0], s_in[1], s_in[2], s_in[3], s_vis[0], s_vis[1], level - 1,
+                                    (float)a.g.V, (float)a.g.E);
+        __syncwarp();
+        if (d.mode == DO_SELECTOR) pull = selector_pull_warp(wsel, s_x, s_x + 16);
+      }
+      if (l == 0) {
+        s_pull = pull;
+        if (blockIdx.x == 0) {
+          a.cnt3[(level + 1) % 3] = 0;
+          if (d.stats)
+            for (int i = 0; i < 4; ++i) d.lstat[4 * ((level + 1) % 3) + i] = 0ull;
+          if (logged) {
+            if (level - 1 < d.max_log)
+              for (int i = 0; i < kSelectorFeatures; ++i) d.feat_log[(level - 1) * kSelectorFeatures + i] = s_x[i];
+            d.time_log[level - 1] = globaltimer_ns();
+          }
+        }
       }
     }
     __syncthreads();
-    bool pull;
-    if (d.mode == DO_FORCE_PUSH)
-      pull = false;
-    else if (d.mode == DO_FORCE_PULL)
-      pull = true;
-    else if (d.mode == DO_SELECTOR)
-      pull = selector_pull(d.sel, s_x, s_x + kSelIn);
-    else
-      pull = ((float)n <= d.threshold * (float)a.g.V) == (d.small_pull != 0);
-    if (logged && blockIdx.x == 0 && threadIdx.x == 0) {
-      if (level - 1 < d.max_log)
-        for (int i = 0; i < kSelectorFeatures; ++i) d.feat_log[(level - 1) * kSelectorFeatures + i] = s_x[i];
-      d.time_log[level - 1] = globaltimer_ns();
-    }
+    const bool pull = s_pull != 0;
+    DoStat *stat = d.stats ? &s_stat : nullptr;
     const DOut out = sparse_out(a, (level & 1) ? a.q1 : a.q0, level);
     if (!pull) {
       const Enum en{(level & 1) ? a.q0 : a.q1, nullptr, n};
-      const EdgeF<UBfsNote, false> f{UBfsNote{a.vd.parent, a.vd.depth, a.g.off, s_stat, level},
+      const EdgeF<UBfsNote, false> f{UBfsNote{a.vd.parent, a.vd.depth, a.g.off, stat, level},
                                      DIn{IN_ALL, nullptr, nullptr}, DIn{IN_ALL, nullptr, nullptr}, true};
       run_lb<LB>(a.g, en, n, f, out, smem, blockIdx.x, gridDim.x);
     } else {
@@ -434,19 +475,20 @@ __global__ void __launch_bounds__(kBfsDoMaxCta, 3) k_bfs_do(DoKernelArgs ka) {
           a.vd.parent[v] = hit;
           a.vd.depth[v] = level;
           out.sparse(v);
-          const unsigned long long k = (unsigned long long)(__ldg(a.g.off + v + 1) - __ldg(a.g.off + v));
-          atomicAdd(s_stat, k);
-          atomicAdd(s_stat + 1, k * k);
-          atomicMax(s_stat + 2, k);
+          if (stat) do_note(stat, (uint32_t)(__ldg(a.g.off + v + 1) - __ldg(a.g.off + v)));
         }
       }
     }
     __syncthreads();
-    if (threadIdx.x == 0 && (s_stat[0] | s_stat[2])) {
-      unsigned long long *nx = d.lstat + 4 * (level % 3);
-      atomicAdd(nx, s_stat[0]);
-      atomicAdd(nx + 1, s_stat[1]);
-      atomicMax(nx + 2, s_stat[2]);
+    if (d.stats && threadIdx.x == 0) {
+      s_vis[0] = fminf((float)a.g.V, s_vis[0] + s_in[0]);
+      s_vis[1] = fminf((float)a.g.E, s_vis[1] + s_in[1]);
+      if (s_stat.sum | s_stat.mx) {
+        unsigned long long *nx = d.lstat + 4 * (level % 3);
+        atomicAdd(nx, (unsigned long long)s_stat.sum);
+        atomicAdd(reinterpret_cast<double *>(nx + 1), (double)s_stat.sq);
+        atomicMax(nx + 2, (unsigned long long)s_stat.mx);
+      }
     }
     clk.tick(a.stop);
     if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
@@ -462,18 +504,26 @@ __global__ void __launch_bounds__(kBfsDoMaxCta, 3) k_bfs_do(DoKernelArgs ka) {
 // two slots cleared.
 __global__ void k_bfs_do_seed(const int32_t *__restrict__ q, int32_t n0, const int32_t *__restrict__ off,
                               unsigned long long *lstat) {
-  __shared__ unsigned long long s[3];
-  if (threadIdx.x < 3) s[threadIdx.x] = 0ull;
+  __shared__ unsigned long long s[2];
+  __shared__ double sq;
+  if (threadIdx.x < 2) s[threadIdx.x] = 0ull;
+  if (threadIdx.x == 0) sq = 0.0;
   __syncthreads();
   for (int32_t i = threadIdx.x; i < n0; i += blockDim.x) {
     const int32_t v = q[i];
     const unsigned long long k = (unsigned long long)(off[v + 1] - off[v]);
     atomicAdd(s, k);
-    atomicAdd(s + 1, k * k);
-    atomicMax(s + 2, k);
+    atomicAdd(&sq, (double)k * (double)k);
+    atomicMax(s + 1, k);
   }
   __syncthreads();
-  if (threadIdx.x < 12) lstat[threadIdx.x] = threadIdx.x < 3 ? s[threadIdx.x] : 0ull;
+  if (threadIdx.x < 12) {
+    unsigned long long v = 0ull;
+    if (threadIdx.x == 0) v = s[0];
+    if (threadIdx.x == 1) v = (unsigned long long)__double_as_longlong(sq);
+    if (threadIdx.x == 2) v = s[1];
+    lstat[threadIdx.x] = v;
+  }
 }
 
 gg_status fused_bfs_do(gg_graph *g, const BfsDoPlan &p, int32_t n0, const VData &vd, gg_frontier *f,
@@ -498,18 +548,20 @@ gg_status fused_bfs_do(gg_graph *g, const BfsDoPlan &p, int32_t n0, const VData 
   ka.d.lstat = static_cast<unsigned long long *>(ls);
   ka.d.sel = p.mode == DO_SELECTOR ? selector_params(p.sel) : nullptr;
   ka.d.mode = p.mode;
+  ka.d.stats = p.mode == DO_SELECTOR || p.feat_log;
   ka.d.threshold = p.threshold;
   ka.d.small_pull = p.small_pull;
   ka.d.feat_log = p.feat_log;
   ka.d.time_log = p.time_log;
   ka.d.max_log = p.max_log;
   const int cta = s->cta_size;
-  const size_t sm = lb_smem(s->load_balancing, cta);
+  uint32_t lbb = (uint32_t)lb_smem(s->load_balancing, cta);
+  const size_t sm = p.mode == DO_SELECTOR ? do_lb_smem_aligned(lbb) + sizeof(float) * kSelectorParams : lbb;
   switch (s->load_balancing) {
-    case GG_LB_VERTEX_BASED: GG_TRY(coop_launch(g, k_bfs_do<GG_LB_VERTEX_BASED>, cta, sm, ka)); break;
-    case GG_LB_WM: GG_TRY(coop_launch(g, k_bfs_do<GG_LB_WM>, cta, sm, ka)); break;
-    case GG_LB_TWCE: GG_TRY(coop_launch(g, k_bfs_do<GG_LB_TWCE>, cta, sm, ka)); break;
-    default: GG_TRY(coop_launch(g, k_bfs_do<GG_LB_CM>, cta, sm, ka)); break;
+    case GG_LB_VERTEX_BASED: GG_TRY(coop_launch(g, k_bfs_do<GG_LB_VERTEX_BASED>, cta, sm, ka, lbb)); break;
+    case GG_LB_WM: GG_TRY(coop_launch(g, k_bfs_do<GG_LB_WM>, cta, sm, ka, lbb)); break;
+    case GG_LB_TWCE: GG_TRY(coop_launch(g, k_bfs_do<GG_LB_TWCE>, cta, sm, ka, lbb)); break;
+    default: GG_TRY(coop_launch(g, k_bfs_do<GG_LB_CM>, cta, sm, ka, lbb)); break;
   }
   int64_t np = 0;
   GG_TRY(read_stats(g, iters, &np));

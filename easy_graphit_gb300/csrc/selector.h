@@ -66,6 +66,79 @@ __device__ __forceinline__ void selector_features(float *x, double n, double sd,
   x[11] = (float)(sd / E);
 }
 
+// Feature i (0..11) of selector_features, in single precision: the per-level
+// form used inside persistent loops, where twelve threads compute one each.
+__device__ __forceinline__ float selector_feature(int i, float n, float sd, float sd2, float mx, float vis_v,
+                                                  float vis_e, int32_t level, float V, float E) {
+  E = E > 1.f ? E : 1.f;
+  const float mean = n > 0.f ? sd / n : 0.f;
+  switch (i) {
+    case 0: return log2f(1.f + n) / 32.f;
+    case 1: return log2f(1.f + sd) / 32.f;
+    case 2: return log2f(1.f + fmaxf(0.f, V - vis_v)) / 32.f;
+    case 3: return log2f(1.f + fmaxf(0.f, E - vis_e)) / 32.f;
+    case 4: return log2f(1.f + mean) / 16.f;
+    case 5: return log2f(1.f + mx) / 32.f;
+    case 6: return log2f(1.f + (n > 0.f ? fmaxf(0.f, sd2 / n - mean * mean) : 0.f)) / 64.f;
+    case 7: return (float)min(level, 256) / 256.f;
+    case 8: return log2f(V) / 32.f;
+    case 9: return log2f(1.f + E) / 32.f;
+    case 10: return n / V;
+    default: return sd / E;
+  }
+}
+
+// The network's parameters staged in shared memory once per persistent CTA:
+// weights rounded to bf16 (as the tensor-core forward pass reads them), biases
+// as they are.  kSelectorParams floats.
+__device__ __forceinline__ void selector_stage(const float *__restrict__ p, float *w) {
+  for (int i = threadIdx.x; i < kSelectorParams; i += blockDim.x) {
+    const bool bias = (i >= kSelB1 && i < kSelW2) || (i >= kSelB2 && i < kSelW3) || i >= kSelB3;
+    const float v = __ldg(p + i);
+    w[i] = bias ? v : __bfloat162float(__float2bfloat16_rn(v));
+  }
+}
+
+// Direction head on staged parameters w (selector_stage), computed by one
+// warp (the calling one; all 32 lanes call it) with warp-level
+// synchronisation only: lane l owns hidden units l and l+32 of both layers,
+// layer 2 accumulates its 64 inputs in order, layer 3's two logits are
+// reduced across the lanes in a fixed tree.  x: 12 features; h1: 64 floats of
+// shared memory.  Returns the same answer in every lane (true = PULL), and in
+// every CTA that computes it from the same x.
+__device__ __forceinline__ bool selector_pull_warp(const float *w, const float *x, float *h1) {
+  auto bf = [](float v) { return __bfloat162float(__float2bfloat16_rn(v)); };
+  const int l = threadIdx.x & 31;
+  float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+  for (int k = 0; k < kSelectorFeatures; ++k) {
+    const float xk = bf(x[k]);
+    a0 += xk * w[kSelW1 + k * kSelHidden + l];
+    a1 += xk * w[kSelW1 + k * kSelHidden + l + 32];
+  }
+  h1[l] = bf(fmaxf(a0 + w[kSelB1 + l], 0.f));
+  h1[l + 32] = bf(fmaxf(a1 + w[kSelB1 + l + 32], 0.f));
+  __syncwarp();
+  a0 = 0.f;
+  a1 = 0.f;
+#pragma unroll 8
+  for (int k = 0; k < kSelHidden; ++k) {
+    const float hk = h1[k];
+    a0 += hk * w[kSelW2 + k * kSelHidden + l];
+    a1 += hk * w[kSelW2 + k * kSelHidden + l + 32];
+  }
+  __syncwarp();
+  const float g0 = bf(fmaxf(a0 + w[kSelB2 + l], 0.f)), g1 = bf(fmaxf(a1 + w[kSelB2 + l + 32], 0.f));
+  float z0 = g0 * w[kSelW3 + l * kSelOut] + g1 * w[kSelW3 + (l + 32) * kSelOut];
+  float z1 = g0 * w[kSelW3 + l * kSelOut + 1] + g1 * w[kSelW3 + (l + 32) * kSelOut + 1];
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    z0 += __shfl_xor_sync(0xffffffffu, z0, d);
+    z1 += __shfl_xor_sync(0xffffffffu, z1, d);
+  }
+  return z1 + w[kSelB3 + 1] > z0 + w[kSelB3];
+}
+
 // Direction head of the network on one feature vector x (12 floats), computed
 // by the calling CTA inside a persistent kernel: fp32 accumulation over
 // bf16-rounded operands, as the tensor-core forward pass computes it.  h is

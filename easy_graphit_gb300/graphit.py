@@ -896,23 +896,65 @@ def sssp_multi(g: GraphT, sources, delta: int, schedule=None, fuse=None):
     return dist, _stats(st)
 
 
-def multigraph_batch(parts, app: str, local_sources, delta: int = 32, schedule=None, fuse=True):
-    """Runs BFS or SSSP on many graphs of uneven size in one traversal: the
-    graphs become one disjoint union, each contributes its source, and the
-    union is traversed once.  Returns (list of per-graph results, stats)."""
-    hg, offs = HostGraph.union(parts)
-    g = GraphT(hg)
-    srcs = np.array([offs[i] + int(s) for i, s in enumerate(local_sources)], dtype=np.int32)
+def sssp_parts(g: GraphT, part_begin, sources, delta: int):
+    """SSSP on a disjoint union, one source per part, each part's loop in a CTA
+    of its own (gg_sssp_parts).  part_begin: [nparts + 1] vertex offsets;
+    sources: union ids.  Returns (dist over the union, stats)."""
+    pb = np.ascontiguousarray(part_begin, dtype=np.int32)
+    srcs = np.ascontiguousarray(sources, dtype=np.int32)
+    dist = np.empty(g.num_vertices, dtype=np.int32)
+    st = L.gg_stats()
+    call("gg_sssp_parts", g.handle, _np_ptr(pb), len(srcs), _np_ptr(srcs), delta, _ptr(dist), C.byref(st))
+    return dist, _stats(st)
+
+
+MESH_MAX_DEGREE = 32  # a part whose largest out-degree is at most this counts as a mesh
+
+
+def multigraph_batch(parts, app: str, local_sources, delta: int = 32, schedule=None, fuse=True,
+                     by_class: bool = True):
+    """Runs BFS or SSSP on many graphs of uneven size: the graphs become a
+    disjoint union, each contributes its source, and the union is traversed
+    once.  For SSSP with by_class, the parts are split by class first: meshes
+    (largest out-degree <= MESH_MAX_DEGREE; high diameter, thousands of small
+    buckets) run one CTA per part (sssp_parts), the others as one multi-source
+    traversal of their union on the whole GPU.  Returns (list of per-graph
+    results, stats); stats["loop_ms"] sums the classes' loops."""
     if schedule is None:
         schedule = SimpleGPUSchedule().configLoadBalancing(SimpleGPUSchedule.load_balancing_type.TWCE)
-    if app == "bfs":
-        out, st = bfs_multi(g, srcs, schedule, fuse)
-    elif app == "sssp":
-        out, st = sssp_multi(g, srcs, delta, schedule, fuse)
-    else:
+    if app not in ("bfs", "sssp"):
         raise ValueError(app)
-    g.close()
-    return [out[offs[i]:offs[i + 1]] for i in range(len(parts))], st
+    classes = [(list(range(len(parts))), "multi")]
+    if app == "sssp" and by_class:
+        mesh = {i for i, p in enumerate(parts)
+                if p.num_edges == 0 or int(np.diff(np.asarray(p.offsets)).max()) <= MESH_MAX_DEGREE}
+        rest = [i for i in range(len(parts)) if i not in mesh]
+        classes = [(c, m) for c, m in ((rest, "multi"), (sorted(mesh), "parts")) if c]
+    out = [None] * len(parts)
+    total = None
+    for idx, mode in classes:
+        hg, offs = HostGraph.union([parts[i] for i in idx])
+        g = GraphT(hg)
+        srcs = np.array([offs[k] + int(local_sources[i]) for k, i in enumerate(idx)], dtype=np.int32)
+        if app == "bfs":
+            r, st = bfs_multi(g, srcs, schedule, fuse)
+        elif mode == "parts":
+            r, st = sssp_parts(g, offs, srcs, delta)
+        else:
+            r, st = sssp_multi(g, srcs, delta, schedule, fuse)
+        g.close()
+        for k, i in enumerate(idx):
+            out[i] = r[offs[k]:offs[k + 1]]
+        if total is None:
+            total = dict(st)
+            total["classes"] = []
+        else:
+            for key in ("loop_ms", "device_ms", "vertices_reached", "edges_traversed", "launches"):
+                total[key] += st[key]
+            total["iterations"] = max(total["iterations"], st["iterations"])
+        total["classes"].append({"graphs": len(idx), "loop_ms": st["loop_ms"],
+                                 "mode": "one CTA per part" if mode == "parts" else "one multi-source traversal"})
+    return out, total
 
 
 def bc(g: GraphT, src: int, schedule=None, fuse=None):

@@ -507,6 +507,16 @@ gg_status gg_sssp_multi(gg_graph *g, const gg_app_schedule *s,
                         int32_t *dist_out, gg_stats *stats);
 gg_status gg_sssp_batch(gg_graph *g, const int32_t *sources, int32_t nsrc,
                         int32_t delta, int32_t *dist_out, gg_stats *stats);
+/* SSSP on a disjoint union of graphs (gg_host_graph_union) with one source per
+ * part, every part's delta-stepping loop in a CTA of its own (no reference
+ * counterpart; the batched mode's path for many high-diameter graphs, whose
+ * loops are barrier-bound on the whole GPU).  Part p holds the vertices
+ * [part_begin[p], part_begin[p+1]) and sources[p] (a vertex of the union) lies
+ * in it; an edge that leaves its part gives GG_ERR_INVALID.  dist_out: V int32
+ * (INT_MAX unreached), each part's values equal to its own gg_sssp. */
+gg_status gg_sssp_parts(gg_graph *g, const int32_t *part_begin, int32_t nparts,
+                        const int32_t *sources, int32_t delta, int32_t *dist_out,
+                        gg_stats *stats);
 
 /* Learned per-level schedule of the batched kernels (no reference
  * counterpart): with a selector attached, batched BFS (GG_BATCH_BFS, the only

@@ -113,6 +113,41 @@ def test_multigraph_batch_uneven_graphs(app):
         np.testing.assert_array_equal(r, ref)
 
 
+@pytest.mark.parametrize("delta", [1, 16, 128])
+def test_sssp_parts_one_cta_per_graph(delta):
+    """gg_sssp_parts on a union of grids, paths and small R-MAT graphs: every
+    part's loop in its own CTA, each part's distances equal to Dijkstra's."""
+    from easy_graphit_gb300 import sssp_parts
+    parts = [HostGraph.grid(n, m, seed=300 + n) for n, m in ((1, 1), (3, 50), (40, 40), (97, 13))]
+    parts += [HostGraph.rmat(sc, ef, seed=400 + sc) for sc, ef in ((6, 4), (10, 16), (12, 8))]
+    n = 700  # a weighted path: 700 buckets at delta 1
+    parts.append(HostGraph.from_edges(n, np.arange(n - 1, dtype=np.int32), np.arange(1, n, dtype=np.int32),
+                                      np.full(n - 1, 3, dtype=np.int32), symmetrize=True))
+    hg, offs = HostGraph.union(parts)
+    g = GraphT(hg)
+    local = [int(p.pick_sources(1, seed=i)[0]) if p.num_edges else 0 for i, p in enumerate(parts)]
+    srcs = np.array([offs[i] + s for i, s in enumerate(local)], dtype=np.int32)
+    for _ in range(2):  # twice: the second call must not see the first's state
+        dist, st = sssp_parts(g, offs, srcs, delta)
+        for i, (p, s_) in enumerate(zip(parts, local)):
+            off, dst, w = np.array(p.offsets), np.array(p.dst), np.array(p.weights)
+            np.testing.assert_array_equal(dist[offs[i]:offs[i + 1]], oracle.sssp_dijkstra(off, dst, w, s_))
+        assert st["fused"] == 1 and st["bucket_advances"] > 0
+    g.close()
+
+
+def test_sssp_parts_rejects_edges_across_parts():
+    from easy_graphit_gb300 import _lib as L, sssp_parts
+    hg = HostGraph.grid(8, 8)
+    g = GraphT(hg)
+    with pytest.raises(L.GGError) as e:  # rows 0-3 and 4-7 of one grid are not separate graphs
+        sssp_parts(g, np.array([0, 32, 64]), np.array([0, 40]), 8)
+    assert e.value.status == L.GG_ERR_INVALID
+    with pytest.raises(L.GGError):
+        sssp_parts(g, np.array([0, 64]), np.array([64]), 8)  # source outside its part
+    g.close()
+
+
 @pytest.mark.parametrize("app", ["bfs", "sssp"])
 def test_batch_plan_cuda_graph_replay(app):
     import torch

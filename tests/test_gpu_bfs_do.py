@@ -122,3 +122,38 @@ def test_collect_directions(name):
     assert f[0, 0] == pytest.approx(np.log2(2) / 32)  # one source on the first frontier
     # the first level's frontier is the source; its out-degree is feature 1
     assert f[0, 1] == pytest.approx(np.log2(1 + np.diff(off)[src]) / 32, rel=1e-6)
+
+
+def test_learned_fused_beats_every_fixed_schedule_on_heldout_graphs():
+    """The shipped network (selector_fused_bfs.bin) inside the fused loop
+    against each fixed schedule of its candidate set -- bfs.cpp's PUSH TWCE
+    fused, its hybrid "power" schedule unfused (as the reference runs it) and
+    the same hybrid rule fused -- on R-MAT graphs whose seeds it never saw
+    (training used 101-103, its evaluation 901-902), two sources each: the
+    summed time of the learned runs is below the summed time of every fixed
+    schedule.  Depths are compared as well."""
+    from easy_graphit_gb300 import Selector
+    learned = LearnedGPUSchedule(Selector.pretrained_fused_bfs())
+    plain, plain_fuse = default_schedule("bfs")
+    scheds = {"plain": (plain, plain_fuse), "power_unfused": (power(0.12), False),
+              "power_fused": (power(0.12), True), "learned": (learned, True)}
+    total = dict.fromkeys(scheds, 0.0)
+    for scale, a, seed in ((20, 0.57, 903), (21, 0.65, 904)):
+        b = (0.95 - a) / 2
+        hg = HostGraph.rmat(scale, 16, a=a, b=b, c=b, seed=seed, symmetrize=True)
+        g = GraphT(hg, symmetric=True)
+        off = np.array(hg.offsets)
+        for src in (int(np.argmax(np.diff(off))), int(hg.pick_sources(1, seed=seed)[0])):
+            first = None
+            for name, (s, fz) in scheds.items():
+                best = None
+                for _ in range(5):
+                    d, _, st = bfs(g, src, s, fz)
+                    best = st["device_ms"] if best is None else min(best, st["device_ms"])
+                total[name] += best
+                if first is None:
+                    first = d
+                np.testing.assert_array_equal(d, first)
+        g.close()
+    for name in ("plain", "power_unfused", "power_fused"):
+        assert total["learned"] < total[name], total
