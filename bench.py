@@ -66,6 +66,9 @@ def parse():
     p.add_argument("--autotune-table", metavar="PATH", default=None,
                    help="only tabulate the autotuned launch shapes of the batched kernels per graph size "
                         "(R-MAT 12-22, grids 256-2048) as markdown into PATH, then exit")
+    p.add_argument("--case", choices=sorted(CASES), default=None,
+                   help="only run one small workload of one kernel a few times (for profiler captures), "
+                        "print its times, then exit")
     p.add_argument("--no-configs", action="store_true",
                    help="omit the lines at the other configurations' own sizes (BFS on the "
                         "symmetrized R-MAT 16, PageRank on R-MAT 24, CC on the symmetrized R-MAT 24)")
@@ -915,8 +918,63 @@ def autotune_table(path, delta=32):
     Path(path).write_text(text)
 
 
+def run_case(name, reps=3):
+    """One small workload per kernel, sized for profiler captures (inputs larger
+    than L2, a few GB on the device at most): prints the device times."""
+    from easy_graphit_gb300 import (GraphT, HostGraph, LearnedGPUSchedule, Selector, SimpleGPUSchedule as T,
+                                    bc_batch, bfs, bfs_batch, cc, default_schedule, pagerank,
+                                    set_batch_selector, sssp, sssp_batch)
+    kind, what = CASES[name]
+    if kind == "grid":
+        hg, sym = HostGraph.grid(2048, 2048), False
+    else:
+        hg, sym = HostGraph.rmat(20, 16, symmetrize=kind == "rmat20s"), kind == "rmat20s"
+    g = GraphT(hg, symmetric=sym)
+    off = np.array(hg.offsets)
+    hub = int(np.argmax(np.diff(off)))
+    srcs = np.ascontiguousarray(hg.pick_sources(64), dtype=np.int32)
+    times = []
+    for _ in range(reps):
+        if what == "sssp_single":
+            sch, fz = default_schedule("sssp")
+            st = sssp(g, int(srcs[0]), 32, sch, fz)[1]
+        elif what == "sssp_batch":
+            st = sssp_batch(g, srcs[:32], 32)[1]
+        elif what == "bfs_learned_fused":
+            st = bfs(g, hub, LearnedGPUSchedule(Selector.pretrained_fused_bfs()), True)[2]
+        elif what == "bfs_batch_learned":
+            set_batch_selector(g, "bfs", Selector.pretrained_batched_bfs())
+            st = bfs_batch(g, srcs)[1]
+        elif what == "bc_batch":
+            st = bc_batch(g, srcs)[1]
+        elif what == "pr_static_pull":
+            st = pagerank(g, 20, 0.85, T().configDirection(T.direction_type.PULL)
+                          .configLoadBalancing(T.load_balancing_type.TWC))[1]
+        elif what == "cc_fused":
+            st = cc(g, None, True)[1]
+        times.append(round(st["loop_ms"] or st["device_ms"], 3))
+    print(json.dumps({"case": name, "V": hg.num_vertices, "E": hg.num_edges, "loop_ms": times}))
+    g.close()
+
+
+# name -> (graph, workload) of run_case
+CASES = {
+    "sssp_grid2048_single": ("grid", "sssp_single"),
+    "sssp_grid2048_batched": ("grid", "sssp_batch"),
+    "sssp_rmat20_batched": ("rmat20", "sssp_batch"),
+    "bfs_rmat20s_learned_fused": ("rmat20s", "bfs_learned_fused"),
+    "bfs_rmat20_batched_learned": ("rmat20", "bfs_batch_learned"),
+    "bc_rmat20s_batched": ("rmat20s", "bc_batch"),
+    "pr_rmat20_static_pull": ("rmat20", "pr_static_pull"),
+    "cc_rmat20s_fused": ("rmat20s", "cc_fused"),
+}
+
+
 def main():
     args = parse()
+    if args.case:
+        run_case(args.case)
+        return
     if args.autotune_table:
         autotune_table(args.autotune_table)
         return
