@@ -320,70 +320,105 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64
         }
       }
     }
-    // (b) busy entries: lane = source, one entry at a time.  The distance
-    // lines of 32 edges are gathered into the warp's shared buffer with
-    // cp.async (one round trip per 32 edges, no registers held); lane t then
-    // collects edge t's near / far source masks and updates its vertex.
+    // (b) busy entries: lane = source, one entry at a time, in groups of 32
+    // edges.  The distance lines of a group's 32 edges are gathered into the
+    // warp's shared buffer with cp.async (one round trip, no registers held);
+    // lane t then collects edge t's near / far source masks and updates its
+    // vertex.  The next group's edge ids and weights (and, at the start of an
+    // entry, the entry's own distances) are loaded before the current
+    // gather is waited for, so that round trip overlaps it.
     uint32_t dense = __ballot_sync(kFull, !sparse && cnt > 0);
     int32_t fmin = INT_MAX;  // lane = source: smallest far value this warp produced
-    while (dense) {
+    int32_t cu = 0, ck = 0, cend = 0, du = INT_MAX, vv = 0, ww = 0;
+    bool have = false, live = false;
+    // next group: same entry (ck + 32 < cend) or the next dense entry
+    auto load_group = [&](int32_t k0, int32_t kend, int32_t &v_, int32_t &w_) {
+      v_ = 0;
+      w_ = 0;
+      if (k0 + lane < kend) {
+        v_ = __ldg(S.dst + k0 + lane);
+        w_ = __ldg(S.w + k0 + lane);
+      }
+    };
+    auto open_entry = [&](int32_t j, int32_t &u_, int32_t &k_, int32_t &e_, int32_t &du_, bool &live_) {
+      u_ = __shfl_sync(kFull, u, j);
+      k_ = __shfl_sync(kFull, b, j);
+      e_ = k_ + __shfl_sync(kFull, cnt, j);
+      const bool act = (__shfl_sync(kFull, m, j) >> lane) & 1u;
+      du_ = act ? __ldcg(S.dist + (int64_t)u_ * kLanes + lane) : INT_MAX;
+      live_ = act;
+    };
+    if (dense) {
       const int32_t j = __ffs(dense) - 1;
       dense &= dense - 1;
-      const int32_t uj = __shfl_sync(kFull, u, j);
-      const int32_t bj = __shfl_sync(kFull, b, j);
-      const int32_t eend = bj + __shfl_sync(kFull, cnt, j);
-      const uint32_t mj = __shfl_sync(kFull, m, j);
-      const bool act = (mj >> lane) & 1u;
-      const int32_t du = act ? __ldcg(S.dist + (int64_t)uj * kLanes + lane) : INT_MAX;
-      const bool live = act && du != INT_MAX;
-      for (int32_t k0 = bj; k0 < eend; k0 += 32) {
-        int32_t vv = 0, ww = 0;
-        if (k0 + lane < eend) {
-          vv = __ldg(S.dst + k0 + lane);
-          ww = __ldg(S.w + k0 + lane);
-        }
-        const int32_t cn = min(32, eend - k0);
-        // lane l copies sources 4(l%8) .. 4(l%8)+3 of edge q + l/8
-        for (int32_t q = 0; q < cn; q += 4) {
-          const int32_t t = q + (lane >> 3);
-          const int32_t vt = __shfl_sync(kFull, vv, t & 31);
-          if (t < cn) cp_async16(dl + t * kLanes + (lane & 7) * 4, S.dist + (int64_t)vt * kLanes + (lane & 7) * 4);
-        }
-        cp_async_wait_all();
-        __syncwarp();
-        uint32_t my_nb = 0, my_fb = 0;
-        for (int32_t t = 0; t < cn; ++t) {
-          const int32_t vt = __shfl_sync(kFull, vv, t);
-          const int32_t wt = __shfl_sync(kFull, ww, t);
-          bool near = false, farb = false;
-          if (live) {
-            const int32_t np = du + wt;
-            if (np < dl[t * kLanes + lane]) {
-              red_min(S.dist + (int64_t)vt * kLanes + lane, np);
-              near = np < cut;
-              farb = !near;
-              if (farb && np < fmin) fmin = np;
-            }
-          }
-          const uint32_t nb = __ballot_sync(kFull, near);
-          const uint32_t fb = __ballot_sync(kFull, farb);
-          if (lane == t) {
-            my_nb = nb;
-            my_fb = fb;
-          }
-        }
-        __syncwarp();  // the buffer is refilled by the next group
-        if (scan) {
-          if (my_nb) red_or(S.nacc + vv, my_nb);
-          if (my_fb) red_or(S.far + vv, my_fb);
+      open_entry(j, cu, ck, cend, du, live);
+      load_group(ck, cend, vv, ww);
+      have = true;
+    }
+    while (have) {
+      const int32_t cn = min(32, cend - ck);
+      // lane l copies sources 4(l%8) .. 4(l%8)+3 of edge q + l/8
+      for (int32_t q = 0; q < cn; q += 4) {
+        const int32_t t = q + (lane >> 3);
+        const int32_t vt = __shfl_sync(kFull, vv, t & 31);
+        if (t < cn) cp_async16(dl + t * kLanes + (lane & 7) * 4, S.dist + (int64_t)vt * kLanes + (lane & 7) * 4);
+      }
+      // the next group's loads, issued before the wait
+      int32_t nu = cu, nk = ck + 32, nend = cend, ndu = du, nvv = 0, nww = 0;
+      bool nlive = live, nhave = true;
+      if (nk >= cend) {
+        if (dense) {
+          const int32_t j = __ffs(dense) - 1;
+          dense &= dense - 1;
+          open_entry(j, nu, nk, nend, ndu, nlive);
         } else {
-          if (my_nb && atomicOr(S.nacc + vv, my_nb) == 0u) {
-            S.qstamp[vv] = it;
-            bs_enqueue_first(S, qo, qcnt_out, vv);
-          }
-          if (my_fb && atomicOr(S.far + vv, my_fb) == 0u) bs_far_push(S, p, vv);
+          nhave = false;
         }
       }
+      if (nhave) load_group(nk, nend, nvv, nww);
+      cp_async_wait_all();
+      __syncwarp();
+      const bool lv = live && du != INT_MAX;
+      uint32_t my_nb = 0, my_fb = 0;
+      for (int32_t t = 0; t < cn; ++t) {
+        const int32_t vt = __shfl_sync(kFull, vv, t);
+        const int32_t wt = __shfl_sync(kFull, ww, t);
+        bool near = false, farb = false;
+        if (lv) {
+          const int32_t np = du + wt;
+          if (np < dl[t * kLanes + lane]) {
+            red_min(S.dist + (int64_t)vt * kLanes + lane, np);
+            near = np < cut;
+            farb = !near;
+            if (farb && np < fmin) fmin = np;
+          }
+        }
+        const uint32_t nb = __ballot_sync(kFull, near);
+        const uint32_t fb = __ballot_sync(kFull, farb);
+        if (lane == t) {
+          my_nb = nb;
+          my_fb = fb;
+        }
+      }
+      __syncwarp();  // the buffer is refilled by the next group
+      if (scan) {
+        if (my_nb) red_or(S.nacc + vv, my_nb);
+        if (my_fb) red_or(S.far + vv, my_fb);
+      } else {
+        if (my_nb && atomicOr(S.nacc + vv, my_nb) == 0u) {
+          S.qstamp[vv] = it;
+          bs_enqueue_first(S, qo, qcnt_out, vv);
+        }
+        if (my_fb && atomicOr(S.far + vv, my_fb) == 0u) bs_far_push(S, p, vv);
+      }
+      cu = nu;
+      ck = nk;
+      cend = nend;
+      du = ndu;
+      live = nlive;
+      vv = nvv;
+      ww = nww;
+      have = nhave;
     }
     if (fmin != INT_MAX && fmin < *(volatile int32_t *)(s_fmin + lane)) atomicMin(s_fmin + lane, fmin);
   }
