@@ -900,12 +900,22 @@ def autotune_table(path, delta=32):
             sym = app == "bc" or (kind == "grid" and app == "bfs")  # grid weights differ per direction
             hg = HostGraph.rmat(size, 16, symmetrize=sym) if kind == "rmat" else HostGraph.grid(size, size)
             g = GraphT(hg, symmetric=sym)
+            name = (f"R-MAT {size}{' sym' if sym else ''}" if kind == "rmat" else f"grid {size}x{size}")
+            if kind == "grid" and app == "sssp":  # meshes: one CTA per source, no launch shape to tune
+                from easy_graphit_gb300 import sssp_batch
+                srcs = hg.pick_sources(nsrc)
+                sssp_batch(g, srcs, delta)
+                ms = min(sssp_batch(g, srcs, delta)[1]["loop_ms"] for _ in range(2))
+                lines.append(f"| {name} | {hg.num_vertices} | {hg.num_edges} | {app} | {nsrc} | "
+                             f"one CTA per source | - | - | - | {ms:.3f} | - | 0 |")
+                print(lines[-1], flush=True)
+                g.close()
+                continue
             best, rows = autotune_batch(g, app, hg.pick_sources(nsrc), delta)
             fit = max(t["blocks_per_sm"] for t, _ in rows)
             ms = min(m for t, m in rows if t == best)
             base = next((m for t, m in rows if t["blocks_per_sm"] == fit and t["chunk"] in (0, 256)
                          and t["edge_parallel_max"] in (0, 6) and t["bottom_up_div"] in (0, 16)), None)
-            name = (f"R-MAT {size}{' sym' if sym else ''}" if kind == "rmat" else f"grid {size}x{size}")
             lines.append(f"| {name} | {hg.num_vertices} | {hg.num_edges} | {app} | {nsrc} | "
                          f"{best['blocks_per_sm']} | {best['chunk'] if app != 'bfs' else '-'} | "
                          f"{best['edge_parallel_max'] if app == 'sssp' else '-'} | "

@@ -262,21 +262,44 @@ __device__ __forceinline__ void bs_relax(const BsState &S, int64_t n_main, int64
       }
       const int32_t total = __shfl_sync(kFull, incl, 31);
       const int32_t excl = incl - sc;
-      for (int32_t t0 = 0; t0 < total; t0 += 32) {
-        const int32_t idx = t0 + lane;
-        int32_t j = 0;  // the last entry whose exclusive offset is <= idx
+      // lane -> (entry, edge) of flattened position idx: the last entry whose
+      // exclusive offset is <= idx
+      auto locate = [&](int32_t idx, int32_t &uj, int32_t &k, uint32_t &mj) {
+        int32_t j = 0;
 #pragma unroll
         for (int st = 16; st > 0; st >>= 1) {
           const int32_t ex = __shfl_sync(kFull, excl, j + st);
           if (ex <= idx) j += st;
         }
-        const int32_t uj = __shfl_sync(kFull, u, j);
-        const int32_t bj = __shfl_sync(kFull, b, j);
-        const int32_t exj = __shfl_sync(kFull, excl, j);
-        const uint32_t mj = __shfl_sync(kFull, m, j);
+        uj = __shfl_sync(kFull, u, j);
+        k = __shfl_sync(kFull, b, j) + (idx - __shfl_sync(kFull, excl, j));
+        mj = __shfl_sync(kFull, m, j);
+      };
+      // the next 32 positions' edge ids and weights are loaded before this
+      // group's distances are compared (one round trip of each group overlaps)
+      int32_t nuj = 0, nv = 0, nw = 0;
+      uint32_t nmj = 0;
+      if (total > 0) {
+        int32_t k;
+        locate(lane, nuj, k, nmj);
+        if (lane < total) {
+          nv = __ldg(S.dst + k);
+          nw = __ldg(S.w + k);
+        }
+      }
+      for (int32_t t0 = 0; t0 < total; t0 += 32) {
+        const int32_t idx = t0 + lane;
+        const int32_t uj = nuj, v = nv, w = nw;
+        const uint32_t mj = nmj;
+        if (t0 + 32 < total) {
+          int32_t k;
+          locate(idx + 32, nuj, k, nmj);
+          if (idx + 32 < total) {
+            nv = __ldg(S.dst + k);
+            nw = __ldg(S.w + k);
+          }
+        }
         if (idx < total) {
-          const int32_t k = bj + (idx - exj);
-          const int32_t v = __ldg(S.dst + k), w = __ldg(S.w + k);
           // the entry's sources four at a time: their u and v distance loads
           // are issued together
           uint32_t mm = mj;
