@@ -552,11 +552,19 @@ def other_configs(peak):
     for _ in range(5):
         oracle.bfs_omp(off, dst, src, threads)
     t = (time.perf_counter() - t0) / 5
+    lines = bfs_single_lines(g, off, dst, src)
+    vr = int((d >= 0).sum())
+    l2 = l2_copy_gbs()
+    fastest = min((v for k, v in lines.items() if isinstance(v, dict)), key=lambda v: v["ms"])
     res["bfs_rmat16_symmetrized"] = {
         "V": hg.num_vertices, "E": hg.num_edges, "source": "highest degree",
         "plain_gteps": er / st["device_ms"] / 1e6, "learned_gteps": er / st2["device_ms"] / 1e6,
         "exact": ok and bool(np.array_equal(d2, d)),
-        "schedules": bfs_single_lines(g, off, dst, src),
+        "schedules": lines,
+        "roofline_l2": {"achieved": (8.0 * er + 16.0 * vr) / (fastest["ms"] / 1e3) / 1e9, "peak": l2,
+                        "unit": "GB/s", "frac": (8.0 * er + 16.0 * vr) / (fastest["ms"] / 1e3) / 1e9 / l2,
+                        "bytes_model": "8 E_r + 16 V_r, fastest schedule's trial time",
+                        "peak_kind": "L2 copy bandwidth measured here (64 MB working set, torch copy_)"},
         "cpu_port": {"gteps": er / t / 1e9, "cores": threads, "sample": "OpenMP port of bfs.cpp, mean of 5"},
         "note": "PUSH TWCE fused (bfs.cpp default); graph L2-resident"}
     g.close()
@@ -640,6 +648,27 @@ def bfs_single_lines(g, off, dst, src, reps=5):
     if "learned_fused" in out:
         out["learned_fused_over_best_fixed"] = out["learned_fused"]["gteps"] / fixed
     return out
+
+
+def l2_copy_gbs(mb=32, reps=50):
+    """Copy bandwidth with a working set that stays in L2 (two buffers of `mb`
+    MB, well under the 129 MB L2): read + write bytes over CUDA-event time,
+    best of three bursts."""
+    import torch
+    a = torch.empty(mb << 18, dtype=torch.float32, device="cuda")
+    b = torch.empty_like(a)
+    for _ in range(5):
+        b.copy_(a)
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            b.copy_(a)
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2.0 * a.numel() * 4 * reps / (e0.elapsed_time(e1) / 1e3) / 1e9)
+    return best
 
 
 def roof_line(alg_bytes, ms, peak, model):

@@ -367,9 +367,11 @@ struct UBfsNote {
   int32_t level;
   __device__ __forceinline__ bool filter(int32_t v) const { return vload(parent + v) == -1; }
   __device__ __forceinline__ bool apply(int32_t s, int32_t d, int32_t) const {
+    // the degree is loaded alongside the CAS (not after it): one round trip
+    const int32_t o0 = stat ? __ldg(off + d) : 0, o1 = stat ? __ldg(off + d + 1) : 0;
     if (!cas(parent + d, -1, s)) return false;
     depth[d] = level;
-    if (stat) do_note(stat, (uint32_t)(__ldg(off + d + 1) - __ldg(off + d)));
+    if (stat) do_note(stat, (uint32_t)(o1 - o0));
     return true;
   }
 };
@@ -458,6 +460,7 @@ __global__ void __launch_bounds__(kBfsDoMaxCta, 4) k_bfs_do(DoKernelArgs ka, uin
            v += (gridDim.x * blockDim.x) >> 3) {
         if (__ldcg(a.vd.parent + v) != -1) continue;
         const int32_t kb = __ldg(d.t.off + v), ke = __ldg(d.t.off + v + 1);
+        const int32_t deg = stat && sub == 0 ? __ldg(a.g.off + v + 1) - __ldg(a.g.off + v) : 0;
         int32_t hit = -1;
         for (int32_t k0 = kb; k0 < ke; k0 += 8) {
           int32_t u = -1;
@@ -475,7 +478,7 @@ __global__ void __launch_bounds__(kBfsDoMaxCta, 4) k_bfs_do(DoKernelArgs ka, uin
           a.vd.parent[v] = hit;
           a.vd.depth[v] = level;
           out.sparse(v);
-          if (stat) do_note(stat, (uint32_t)(__ldg(a.g.off + v + 1) - __ldg(a.g.off + v)));
+          if (stat) do_note(stat, (uint32_t)deg);
         }
       }
     }
