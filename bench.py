@@ -564,7 +564,7 @@ def other_configs(peak):
         "roofline_l2": {"achieved": (8.0 * er + 16.0 * vr) / (fastest["ms"] / 1e3) / 1e9, "peak": l2,
                         "unit": "GB/s", "frac": (8.0 * er + 16.0 * vr) / (fastest["ms"] / 1e3) / 1e9 / l2,
                         "bytes_model": "8 E_r + 16 V_r, fastest schedule's trial time",
-                        "peak_kind": "L2 copy bandwidth measured here (64 MB working set, torch copy_)"},
+                        "peak_kind": "L2 copy bandwidth measured here (16 MB working set, torch copy_)"},
         "cpu_port": {"gteps": er / t / 1e9, "cores": threads, "sample": "OpenMP port of bfs.cpp, mean of 5"},
         "note": "PUSH TWCE fused (bfs.cpp default); graph L2-resident"}
     g.close()
@@ -650,10 +650,10 @@ def bfs_single_lines(g, off, dst, src, reps=5):
     return out
 
 
-def l2_copy_gbs(mb=32, reps=50):
+def l2_copy_gbs(mb=8, reps=200):
     """Copy bandwidth with a working set that stays in L2 (two buffers of `mb`
-    MB, well under the 129 MB L2): read + write bytes over CUDA-event time,
-    best of three bursts."""
+    MB, far under the 129 MB L2, which is split between the two dies): read +
+    write bytes over CUDA-event time, best of three bursts."""
     import torch
     a = torch.empty(mb << 18, dtype=torch.float32, device="cuda")
     b = torch.empty_like(a)
