@@ -687,7 +687,7 @@ def reach_of(deg, rows):
 
 
 def scale24_directed(g, hg, peak):
-    """R-MAT 24 directed (the benchmark spec's 50%-of-HBM scale): batched BFS (64
+    """R-MAT 24 directed (the 50 %-of-HBM target's scale): batched BFS (64
     sources, learned directions), batched SSSP (32 sources, delta 32), and
     single-source BFS (bfs.cpp's schedule) and SSSP (sssp.cpp's and TWCE,
     fused), each with GTEPS and its roofline fraction by the per-app byte
