@@ -73,8 +73,17 @@ struct USssp {
       }
 #pragma unroll
       for (int j = 0; j < B; ++j) prev[j] = d[j] >= 0 ? __ldcg(dist + d[j]) : INT_MIN;
+      // The minimum is a fire-and-forget reduction and the improvement is
+      // decided against the value just read: a distance only decreases, so a
+      // target read at or below np needs nothing, and one read above it is
+      // queued or parked -- redundantly at worst, when a lighter path landed
+      // in between (its own relaxation registers it too).
 #pragma unroll
-      for (int j = 0; j < B; ++j) prev[j] = np[j] < prev[j] ? atomicMin(dist + d[j], np[j]) : INT_MIN;
+      for (int j = 0; j < B; ++j)
+        if (np[j] < prev[j])
+          asm volatile("red.relaxed.gpu.global.min.s32 [%0], %1;" ::"l"(__cvta_generic_to_global(dist + d[j])),
+                       "r"(np[j])
+                       : "memory");
 #pragma unroll
       for (int j = 0; j < B; ++j) {
         if (prev[j] <= np[j]) continue;
