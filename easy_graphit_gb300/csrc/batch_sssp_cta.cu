@@ -99,9 +99,11 @@ __global__ void __launch_bounds__(512) k_sssp_cta(CtaSsspArgs c) {
   a.delta = c.delta;
   a.fill_target = 1024;
   a.width0 = 16;
+  a.rec_mode = 1;
   if (threadIdx.x < BQ_STOP) {
     const int32_t i = threadIdx.x;
-    sctl[i] = i == BQ_NEAR ? 1 : (i >= BQ_MIN && i < BQ_MIN + 3 ? INT_MAX : (i == BQ_FILL ? -1 : 0));
+    const bool big = (i >= BQ_MIN && i < BQ_MIN + 3) || (i >= BQ_REC && i < BQ_REC + 2);
+    sctl[i] = i == BQ_NEAR ? 1 : (big ? INT_MAX : (i == BQ_FILL ? -1 : 0));
   }
   if (threadIdx.x == 0) a.q0[0] = c.srcs[k];
   __syncthreads();
