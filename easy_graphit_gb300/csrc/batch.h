@@ -78,8 +78,7 @@ struct CtaBuffers {
   int32_t *rows = nullptr;   // [k][V] distances
   int32_t *dsrc = nullptr;   // [k]
   int32_t *stats = nullptr;  // [0] most relax steps of a source, [1] bucket advances
-  int32_t *stamp = nullptr, *piles = nullptr, *q = nullptr;
-  int64_t qcap = 0;
+  int32_t *stamp = nullptr, *piles = nullptr;
   int32_t k = 0;
 };
 int32_t bsssp_cta_width(const gg_graph *g);

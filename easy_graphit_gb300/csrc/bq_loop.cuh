@@ -1,6 +1,5 @@
 // The delta-stepping step machine over the bucket queue of bucket_queue.cuh,
-// shared by the persistent single-source loop (fused.cu, k_sssp_bq) and the
-// batched mode that gives every source its own CTA (batch_sssp_cta.cu).
+// run by the persistent single-source loop (fused.cu, k_sssp_bq).
 #pragma once
 
 #include "bucket_queue.cuh"
@@ -63,13 +62,6 @@ struct BqArgs {
   int32_t solo_pile_max;  // largest pile step (pile entries) CTA 0 runs alone
   int32_t fill_target;  // low-pile entries a refill aims for
   int32_t width0;       // first horizon width, in buckets
-  // Recorded-minimum mode (batched runs, which need each source's distances
-  // but not the reference's bucket sequence): parks and splits fold every
-  // low-pile value into a per-generation minimum, and an advance starts its
-  // window there instead of scanning the low pile for the exact minimum.  A
-  // recorded value whose vertex was lowered since makes the window start
-  // early (at worst empty); it never starts late, so no vertex is skipped.
-  int32_t rec_mode;
 };
 
 // Loop state, the same in every CTA: every decision is taken from control
@@ -145,8 +137,7 @@ __device__ __forceinline__ void bq_step(BqLoop &s, const BqArgs &a, const BqStep
   switch (st.kind) {
     case BQ_RELAX: {
       const DFar far{a.b.stamp, a.b.lo[s.g & 1], ctl + BQ_LO + (s.g & 1), a.b.hi[s.gh & 1],
-                     ctl + BQ_HI + (s.gh & 1), bq_lo_tag(s.g), bq_hi_tag(s.gh), s.hz, a.b.V, a.err,
-                     a.rec_mode ? ctl + BQ_REC + (s.g & 1) : nullptr};
+                     ctl + BQ_HI + (s.gh & 1), bq_lo_tag(s.g), bq_hi_tag(s.gh), s.hz, a.b.V, a.err};
       const EdgeF<USssp, false> f{USssp{a.dist, U, far}, DIn{IN_ALL, nullptr, nullptr},
                                   DIn{IN_ALL, nullptr, nullptr}, false};
       const int32_t n = (int64_t)st.work > a.qcap ? (int32_t)a.qcap : st.work;  // past qcap only after a flagged overflow
@@ -162,13 +153,8 @@ __device__ __forceinline__ void bq_step(BqLoop &s, const BqArgs &a, const BqStep
         ctl[BQ_LO + lo_next] = 0;
         ctl[BQ_HI + ((s.gh + 1) & 1)] = 0;
         ctl[BQ_FILL + ((s.gh + 1) & 1)] = 0;
-        if (a.rec_mode) {
-          ctl[BQ_MIN + s.it % 3] = ctl[BQ_REC + (s.g & 1)];
-          ctl[BQ_REC + lo_next] = INT_MAX;
-        }
       }
-      if (!a.rec_mode)
-        bq_pile_min(a.b.lo[s.g & 1], min(st.work, a.b.V), a.dist, U, ctl + BQ_MIN + s.it % 3, rank, nparts, red);
+      bq_pile_min(a.b.lo[s.g & 1], min(st.work, a.b.V), a.dist, U, ctl + BQ_MIN + s.it % 3, rank, nparts, red);
       s.phase = 1;
       break;
     case BQ_LOSPLIT: {
@@ -176,8 +162,7 @@ __device__ __forceinline__ void bq_step(BqLoop &s, const BqArgs &a, const BqStep
       const int32_t n_lo = min(*(volatile int32_t *)(ctl + BQ_LO + (s.g & 1)), a.b.V);
       if (win <= s.hz) {
         const BqSplitOut o{a.b.stamp, a.b.lo[lo_next], ctl + BQ_LO + lo_next, bq_lo_tag(s.g + 1),
-                           nullptr, nullptr, 0, INT_MAX, nullptr, a.b.V, false,
-                           a.rec_mode ? ctl + BQ_REC + lo_next : nullptr};
+                           nullptr, nullptr, 0, INT_MAX, nullptr, a.b.V, false};
         bq_pile_split(a.b.lo[s.g & 1], n_lo, a.dist, U, win, front, o, a.err, rank, nparts);
       } else {
         // the window reaches past the horizon: split both piles under a new one
@@ -185,8 +170,7 @@ __device__ __forceinline__ void bq_step(BqLoop &s, const BqArgs &a, const BqStep
         s.k = bq_adapt_width(s.k, *(volatile int32_t *)(ctl + BQ_FILL + (s.gh & 1)), a.fill_target);
         const int32_t hz = bq_clamp((int64_t)st.m + (int64_t)s.k * a.delta);
         BqSplitOut o{a.b.stamp, a.b.lo[lo_next], ctl + BQ_LO + lo_next, bq_lo_tag(s.g + 1),
-                     a.b.hi[hi_next], ctl + BQ_HI + hi_next, bq_hi_tag(s.gh + 1), hz, nullptr, a.b.V, true,
-                     a.rec_mode ? ctl + BQ_REC + lo_next : nullptr};
+                     a.b.hi[hi_next], ctl + BQ_HI + hi_next, bq_hi_tag(s.gh + 1), hz, nullptr, a.b.V, true};
         bq_pile_split(a.b.lo[s.g & 1], n_lo, a.dist, U, win, front, o, a.err, rank, nparts);
         o.fill = ctl + BQ_FILL + hi_next;
         bq_pile_split(a.b.hi[s.gh & 1], min(*(volatile int32_t *)(ctl + BQ_HI + (s.gh & 1)), a.b.V), a.dist, U,
@@ -207,7 +191,6 @@ __device__ __forceinline__ void bq_step(BqLoop &s, const BqArgs &a, const BqStep
         ctl[BQ_LO + lo_next] = 0;
         ctl[BQ_HI + hi_next] = 0;
         ctl[BQ_FILL + hi_next] = 0;
-        if (a.rec_mode) ctl[BQ_REC + lo_next] = INT_MAX;
       }
       bq_pile_min(a.b.hi[s.gh & 1], min(st.work, a.b.V), a.dist, U, ctl + BQ_MIN + s.it % 3, rank, nparts, red);
       s.phase = 2;
@@ -219,7 +202,7 @@ __device__ __forceinline__ void bq_step(BqLoop &s, const BqArgs &a, const BqStep
       const int32_t hz = bq_clamp((int64_t)st.m + (int64_t)s.k * a.delta);
       const BqSplitOut o{a.b.stamp, a.b.lo[lo_next], ctl + BQ_LO + lo_next, bq_lo_tag(s.g + 1),
                          a.b.hi[hi_next], ctl + BQ_HI + hi_next, bq_hi_tag(s.gh + 1), hz,
-                         ctl + BQ_FILL + hi_next, a.b.V, false, a.rec_mode ? ctl + BQ_REC + lo_next : nullptr};
+                         ctl + BQ_FILL + hi_next, a.b.V, false};
       bq_pile_split(a.b.hi[s.gh & 1], min(st.work, a.b.V), a.dist, U, bq_clamp((int64_t)st.m + a.delta), front,
                     o, a.err, rank, nparts);
       s.cur = st.m;

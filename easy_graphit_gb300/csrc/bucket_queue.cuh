@@ -52,11 +52,10 @@ enum : int32_t {
   BQ_LO = 6,      // [2] low-pile counts, by generation parity
   BQ_HI = 8,      // [2] high-pile counts, by generation parity
   BQ_FILL = 10,   // [2] entries a refill moved to the low pile, by high generation parity
-  BQ_REC = 12,    // [2] recorded minimum of each low-pile generation (recorded-minimum mode)
-  BQ_STOP = 14,   // loop time-limit flag
-  BQ_STATS = 15,  // [2] relax steps, bucket advances
-  BQ_PUB = 17,    // [16] loop state published by the one-CTA mode
-  BQ_CTL_INTS = 48
+  BQ_STOP = 12,   // loop time-limit flag
+  BQ_STATS = 13,  // [2] relax steps, bucket advances
+  BQ_PUB = 16,    // [16] loop state published by the one-CTA mode
+  BQ_CTL_INTS = 32
 };
 
 // Device buffers of one queue: stamps, two generations of each pile, control.
@@ -117,7 +116,6 @@ struct BqSplitOut {
   int32_t *fill;         // optional count of entries sent to the low pile
   int32_t cap;
   bool dedup;            // two piles feed the low pile in this step: append once per vertex
-  int32_t *rec;          // recorded-minimum mode: the low generation's minimum (else null)
 };
 
 // Splits pile[0, n): stale entries (P < U) are dropped, the window
@@ -155,7 +153,6 @@ __device__ __forceinline__ void bq_pile_split(const int32_t *__restrict__ pile, 
         else
           atomicOr(err, DEV_ERR_OVERFLOW);
         if (o.fill) agg_inc(o.fill);
-        if (o.rec) atomicMin(o.rec, p);
       } else {
         o.stamp[v] = o.hi_tag;
         const int32_t pos = agg_inc(o.hi_cnt);

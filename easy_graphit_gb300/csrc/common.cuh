@@ -156,11 +156,9 @@ struct DFar {
   int32_t horizon;          // p < horizon -> low pile
   int32_t cap;              // entries a pile can hold (V)
   int32_t *err;
-  int32_t *rec;             // recorded-minimum mode: low-pile minimum of the generation (else null)
 
   __device__ __forceinline__ void park(int32_t v, int32_t p) const {
     const bool low = p < horizon;
-    if (low && rec) atomicMin(rec, p);  // also when v is listed already: its value dropped
     const int32_t tag = low ? lo_tag : hi_tag;
     if (atomicExch(stamp + v, tag) == tag) return;
     if (low) {

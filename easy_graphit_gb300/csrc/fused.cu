@@ -201,7 +201,7 @@ __global__ void k_bq_init(int32_t *ctl, int32_t n0) {
   if (i >= BQ_CTL_INTS) return;
   int32_t v = 0;
   if (i == BQ_NEAR) v = n0;
-  if ((i >= BQ_MIN && i < BQ_MIN + 3) || (i >= BQ_REC && i < BQ_REC + 2)) v = INT_MAX;
+  if (i >= BQ_MIN && i < BQ_MIN + 3) v = INT_MAX;
   if (i == BQ_FILL) v = -1;
   ctl[i] = v;
 }
