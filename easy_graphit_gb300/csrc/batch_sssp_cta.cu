@@ -79,7 +79,7 @@ __global__ void k_sssp_cta_init(CtaSsspArgs c, int32_t k) {
   }
 }
 
-constexpr int kMeshThreads = 512;
+constexpr int kMeshThreads = 1024;
 constexpr int kMeshList = 2048;          // entries of each shared relax list
 constexpr int kMeshInFlight = 4;         // pile entries / edges a thread keeps in flight
 constexpr int kMeshSlots = 128;          // buckets of the ring (a power of two)
@@ -108,6 +108,7 @@ struct MeshCtl {
   int32_t sp_cnt[2];       // spill piles, by generation parity
   int32_t q_cnt[2];        // overflow queues, by step parity
   int32_t list_cnt[3];     // relax-list counts, rotating by round
+  int32_t rquit[3];        // time limit reached, rotating by round like list_cnt
   int32_t srec;            // smallest live spill value listed since the last advance
   int32_t sdead;           // spill entries the last advance found dead or took
   int32_t himin;           // smallest live far value (MESH_HIMIN)
@@ -401,12 +402,31 @@ __global__ void __launch_bounds__(kMeshThreads) k_sssp_cta(CtaSsspArgs c) {
     mv.q[0][0] = src;
   }
   uint64_t deadline = 0;
-  if (threadIdx.x == 0) deadline = globaltimer_ns() + c.loop_limit_ns;
+  if (threadIdx.x == 0) {
+    deadline = globaltimer_ns() + c.loop_limit_ns;
+    C.kind = -1;  // no step before the first
+  }
   __syncthreads();
   for (;;) {
-    // ---- warp 0 decides the step (lane 0 writes it)
+    // ---- warp 0 closes the last step (lane 0) and decides the next one
     if (threadIdx.x < 32) {
       const int lane = threadIdx.x;
+      if (lane == 0) {
+        const int32_t last = C.kind;
+        if (last >= 0) C.steps++;
+        if (last == MESH_ADV || last == MESH_HISPLIT) {
+          C.adv++;
+          if (last == MESH_ADV) C.rc[C.nJ & (kMeshSlots - 1)] = 0;  // the bucket's slot is consumed
+          C.J = C.nJ;
+          C.U = C.win;
+          C.gh = C.gh_w;
+          C.gs = C.gs_w;
+        }
+        if (last == MESH_RELAX || last == MESH_ADV || last == MESH_HISPLIT) C.in ^= 1;
+        if (last == MESH_HIMIN) C.after_himin = 1;
+        if (last == MESH_COMPACT) C.gs = C.gs_w;
+      }
+      __syncwarp();
       // the next ring bucket that holds entries, if any: (J, Jend) in steps of 32
       const int32_t span = min(C.Jend - C.J - 1, kMeshSlots - 1);
       int32_t jr = INT_MAX;
@@ -424,7 +444,7 @@ __global__ void __launch_bounds__(kMeshThreads) k_sssp_cta(CtaSsspArgs c) {
         if ((C.steps & 255) == 0) {  // the wall-clock bound and overflow, checked every 256 steps
           const bool late = globaltimer_ns() > deadline;
           if (late) atomicOr(c.err, DEV_ERR_TIMEOUT);
-          C.quit = late || (*(volatile int32_t *)c.err & (DEV_ERR_OVERFLOW | DEV_ERR_TIMEOUT)) != 0;
+          C.quit = C.quit || late || (*(volatile int32_t *)c.err & (DEV_ERR_OVERFLOW | DEV_ERR_TIMEOUT)) != 0;
         }
         C.nq = min(C.q_cnt[C.in], (int32_t)mv.qcap);
         C.gh_w = C.gh;
@@ -477,6 +497,8 @@ __global__ void __launch_bounds__(kMeshThreads) k_sssp_cta(CtaSsspArgs c) {
         C.q_cnt[C.in ^ 1] = 0;
         C.list_cnt[0] = 0;
         C.list_cnt[1] = 0;
+        C.rquit[0] = 0;
+        C.rquit[1] = 0;
       }
     }
     __syncthreads();
@@ -496,37 +518,33 @@ __global__ void __launch_bounds__(kMeshThreads) k_sssp_cta(CtaSsspArgs c) {
     s.q = in ? mv.q[0] : mv.q[1];
     s.q_cnt = &C.q_cnt[in ^ 1];
     int32_t smin = INT_MAX;  // smallest value this thread left on a spill pile
-    if (kind == MESH_HIMIN || kind == MESH_COMPACT) {
-      if (kind == MESH_HIMIN) {
-        // smallest live value of the far pile (everything at or above the cutoff)
-        const int32_t *pile = (C.gh & 1) ? mv.far[1] : mv.far[0];
-        const int32_t nf = C.nfar, U = C.U;
-        int32_t mn = INT_MAX;
-        for (int32_t i0 = threadIdx.x; i0 < nf; i0 += kMeshInFlight * blockDim.x) {
-          int32_t v[kMeshInFlight], p[kMeshInFlight];
+    if (kind == MESH_HIMIN) {
+      // smallest live value of the far pile (everything at or above the cutoff)
+      const int32_t *pile = (C.gh & 1) ? mv.far[1] : mv.far[0];
+      const int32_t nf = C.nfar, U = C.U;
+      int32_t mn = INT_MAX;
+      for (int32_t i0 = threadIdx.x; i0 < nf; i0 += kMeshInFlight * blockDim.x) {
+        int32_t v[kMeshInFlight], p[kMeshInFlight];
 #pragma unroll
-          for (int j = 0; j < kMeshInFlight; ++j)
-            v[j] = i0 + j * (int32_t)blockDim.x < nf ? __ldcg(pile + i0 + j * blockDim.x) : -1;
+        for (int j = 0; j < kMeshInFlight; ++j)
+          v[j] = i0 + j * (int32_t)blockDim.x < nf ? __ldcg(pile + i0 + j * blockDim.x) : -1;
 #pragma unroll
-          for (int j = 0; j < kMeshInFlight; ++j) p[j] = v[j] >= 0 ? __ldcg(mv.dist + v[j]) : INT_MAX;
+        for (int j = 0; j < kMeshInFlight; ++j) p[j] = v[j] >= 0 ? __ldcg(mv.dist + v[j]) : INT_MAX;
 #pragma unroll
-          for (int j = 0; j < kMeshInFlight; ++j)
-            if (p[j] >= U) mn = min(mn, p[j]);
-        }
-        mesh_fold_min(mn, &C.himin);
-      } else {
-        // live spill entries (at or above the cutoff) move to a new generation
-        int32_t nd = 0;
-        mesh_scan<KEEP_MOVE>(mv, s, (C.gs & 1) ? mv.sp[1] : mv.sp[0], C.nsp, C.U, C.U, smin, nd);
-        mesh_fold_min(smin, &C.srec);
+        for (int j = 0; j < kMeshInFlight; ++j)
+          if (p[j] >= U) mn = min(mn, p[j]);
       }
+      mesh_fold_min(mn, &C.himin);
       __syncthreads();
-      if (threadIdx.x == 0) {
-        if (kind == MESH_HIMIN) C.after_himin = 1;
-        else C.gs = C.gs_w;
-        C.steps++;
-      }
-      continue;  // the next decision reads what this step folded, after the barrier above
+      continue;  // the next decision reads the minimum after the barrier above
+    }
+    if (kind == MESH_COMPACT) {
+      // live spill entries (at or above the cutoff) move to a new generation
+      int32_t nd = 0;
+      mesh_scan<KEEP_MOVE>(mv, s, (C.gs & 1) ? mv.sp[1] : mv.sp[0], C.nsp, C.U, C.U, smin, nd);
+      mesh_fold_min(smin, &C.srec);
+      __syncthreads();
+      continue;
     }
     if (kind == MESH_RELAX) {
       // the overflow queue of the last step: window vertices at their current distance
@@ -546,8 +564,15 @@ __global__ void __launch_bounds__(kMeshThreads) k_sssp_cta(CtaSsspArgs c) {
       const int32_t lo = (int32_t)min((int64_t)C.nJ * delta, (int64_t)INT_MAX), win = C.win;
       s.lo = lo;
       if (kind == MESH_ADV) {
-        const int32_t slot = C.nJ & (kMeshSlots - 1);
-        mesh_scan_slot(mv, s, mv.ring + (int64_t)slot * mv.slot_cap, C.nslot);
+        const int4 *slot = mv.ring + (int64_t)(C.nJ & (kMeshSlots - 1)) * mv.slot_cap;
+        const int32_t ns = C.nslot, T = blockDim.x;
+        // the first block-width of entries is relaxed by the thread that reads
+        // it; the rest goes to the relax list (even shares in the first round)
+        if (ns > T) mesh_scan_slot(mv, s, slot + T, ns - T);
+        if ((int32_t)threadIdx.x < ns) {
+          const int4 x = __ldcg(slot + threadIdx.x);
+          mesh_relax(mv, s, x.x, x.y, x.z, x.w, smin);
+        }
         if (C.nsp > 0) {
           int32_t nd = 0;
           mesh_scan<KEEP_STAY>(mv, s, (C.gs & 1) ? mv.sp[1] : mv.sp[0], C.nsp, lo, win, smin, nd);
@@ -558,12 +583,23 @@ __global__ void __launch_bounds__(kMeshThreads) k_sssp_cta(CtaSsspArgs c) {
         mesh_scan<KEEP_SPLIT>(mv, s, (C.gh & 1) ? mv.far[1] : mv.far[0], C.nfar, lo, win, smin, nd);
       }
     }
-    // relax rounds: list r is read in round r + 1, which fills list r + 1
+    // relax rounds: list r is read in round r + 1, which fills list r + 1;
+    // minima of spilled values are folded before every barrier
+    mesh_fold_min(smin, &C.srec);
+    smin = INT_MAX;
     __syncthreads();
     for (int32_t r = 1;; ++r) {
       const int32_t nl = min(C.list_cnt[(r - 1) % 3], kMeshList);
-      if (nl == 0) break;
-      if (threadIdx.x == 0) C.list_cnt[(r + 1) % 3] = 0;
+      if (nl == 0 || C.rquit[(r - 1) % 3]) break;
+      if (threadIdx.x == 0) {
+        C.list_cnt[(r + 1) % 3] = 0;
+        C.rquit[(r + 1) % 3] = 0;
+        if ((r & 63) == 0 && globaltimer_ns() > deadline) {  // the wall-clock bound holds inside a step too
+          atomicOr(c.err, DEV_ERR_TIMEOUT);
+          C.rquit[r % 3] = 1;  // read after this round's barrier
+          C.quit = 1;
+        }
+      }
       const int4 *lin = lists + ((r - 1) & 1) * kMeshList;
       s.list = lists + (r & 1) * kMeshList;
       s.list_cnt = &C.list_cnt[r % 3];
@@ -571,22 +607,10 @@ __global__ void __launch_bounds__(kMeshThreads) k_sssp_cta(CtaSsspArgs c) {
         const int4 x = lin[i];
         mesh_relax(mv, s, x.x, x.y, x.z, x.w, smin);
       }
+      mesh_fold_min(smin, &C.srec);
+      smin = INT_MAX;
       __syncthreads();
     }
-    mesh_fold_min(smin, &C.srec);
-    if (threadIdx.x == 0) {
-      C.steps++;
-      if (kind == MESH_ADV || kind == MESH_HISPLIT) {
-        C.adv++;
-        if (kind == MESH_ADV) C.rc[C.nJ & (kMeshSlots - 1)] = 0;  // the bucket's slot is consumed
-        C.J = C.nJ;
-        C.U = C.win;
-        C.gh = C.gh_w;
-        C.gs = C.gs_w;
-      }
-      C.in ^= 1;
-    }
-    __syncthreads();
   }
   if (threadIdx.x == 0) {
     atomicMax(c.stats, C.steps);
