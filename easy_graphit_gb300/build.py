@@ -100,12 +100,16 @@ def build_oracle() -> Path:
 
 
 def build_ref_oracle() -> Path | None:
-    """Compiles the reference's GAPBS code into oracle/_ref when GG_REF_DIR names
-    a reference tree (machines that only run the tests have none)."""
+    """Compiles the reference's GAPBS code and its five apps (against the
+    oracle's host-execution stand-in for BuildIt) into oracle/_ref when
+    GG_REF_DIR names a reference tree (machines that only run the tests have
+    none)."""
     ref_dir = os.environ.get("GG_REF_DIR")
     if not ref_dir or not (Path(ref_dir) / "runtime" / "infra_gapbs").is_dir():
         return None
     _run(["make", "-s", "-C", str(ORACLE), "ref", f"REF_DIR={ref_dir}"])
+    if (Path(ref_dir) / "apps").is_dir():
+        _run(["make", "-s", "-C", str(ORACLE), "apps", f"REF_DIR={ref_dir}"])
     return ORACLE / "_ref" / "ref_gapbs"
 
 

@@ -36,6 +36,36 @@ def golden():
     return np.load(GOLDEN)
 
 
+APP_GOLDEN = ROOT / "tests" / "golden" / "ref_apps.npz"
+APP_GRAPHS = ["rmat10_k16_sym", "rmat11_k8_dir", "grid32"]
+
+
+@pytest.fixture(scope="session")
+def app_golden():
+    """Outputs of the reference's own apps/*.cpp (tests/golden/make_app_golden.py)."""
+    return np.load(APP_GOLDEN)
+
+
+def app_graph(app_golden, name):
+    """(offsets, dst, w) of a graph of ref_apps.npz: the R-MAT ones rebuilt by
+    the oracle's generator (checked against the stored digest), the grid stored whole."""
+    import hashlib
+
+    import oracle
+
+    if f"graph/{name}/offsets" in app_golden.files:
+        return (app_golden[f"graph/{name}/offsets"], app_golden[f"graph/{name}/dst"],
+                app_golden[f"graph/{name}/w"])
+    off, dst, w = (np.asarray(a, dtype=np.int32) for a in oracle.rmat(
+        int(app_golden[f"graph/{name}/scale"]), int(app_golden[f"graph/{name}/degree"]),
+        symmetrize=bool(app_golden[f"graph/{name}/symmetrize"])))
+    h = hashlib.sha256()
+    for a in (off, dst, w):
+        h.update(np.ascontiguousarray(a, dtype=np.int32).tobytes())
+    assert h.hexdigest() == str(app_golden[f"graph/{name}/sha256"]), name
+    return off, dst, w
+
+
 def rel_l1(x, ref):
     x = np.asarray(x, dtype=np.float64)
     ref = np.asarray(ref, dtype=np.float64)

@@ -333,3 +333,37 @@ def test_cc_fused_when_the_giant_tree_joins_a_smaller_root_late(symmetrize):
     np.testing.assert_array_equal(fused, ref)
     assert fused[3000] == 0 and fused[4999] == 0 and fused[500] == 500 and fused[5005] == 5000
     g.close()
+
+
+# ------------------------------------------------- the reference's own apps
+@pytest.mark.parametrize("name", ["rmat10_k16_sym", "rmat11_k8_dir", "grid32"])
+def test_engine_matches_the_reference_apps(app_golden, name):
+    """The engine against what easy_graphit's own apps/*.cpp compute on the
+    same graphs (tests/golden/ref_apps.npz, made by running those sources on
+    the CPU): each app's default schedule and the batched / fused forms."""
+    from easy_graphit_gb300 import bc_batch, bfs_batch, sssp_batch
+    from tests.conftest import app_graph
+    off, dst, w = app_graph(app_golden, name)
+    g = GraphT(HostGraph.from_csr(off, dst, w), symmetric=name.endswith("_sym"))
+    srcs = [int(s) for s in app_golden[f"sources/{name}"]]
+    want = app_golden[f"pr/{name}"]
+    r, _ = pagerank(g, 20, 0.85)  # pr.cpp's PULL EDGE_ONLY blocked schedule
+    assert rel_l1(r, want) <= PR_TOL, rel_l1(r, want)
+    r, _ = pagerank(g, 20, 0.85, sched(direction=T.direction_type.PULL, lb=T.load_balancing_type.TWC))
+    assert rel_l1(r, want) <= PR_TOL, rel_l1(r, want)
+    np.testing.assert_array_equal(cc(g)[0], app_golden[f"cc/{name}"])
+    np.testing.assert_array_equal(cc(g, None, True)[0], app_golden[f"cc/{name}"])
+    rows, _ = bc_batch(g, srcs)
+    for k, s in enumerate(srcs):
+        want = app_golden[f"bc/{name}/s{k}"]
+        dep, _ = bc(g, s)
+        assert rel_l1(dep, want) <= BC_TOL, (s, rel_l1(dep, want))
+        assert rel_l1(rows[k], want) <= BC_TOL, (s, rel_l1(rows[k], want))
+    want = app_golden[f"bfs/{name}"]
+    np.testing.assert_array_equal(bfs(g, srcs[0])[0], want)
+    np.testing.assert_array_equal(bfs_batch(g, srcs[:1])[0][0], want)
+    for d in (1, 8, 32):
+        want = app_golden[f"sssp/{name}/d{d}"]
+        np.testing.assert_array_equal(sssp(g, srcs[0], d)[0], want)
+        np.testing.assert_array_equal(sssp_batch(g, srcs[:1], d)[0][0], want)
+    g.close()

@@ -207,3 +207,63 @@ def test_pagerank_matches_sparse_power_iteration(golden, name):
         contrib = np.divide(r, outdeg, out=np.zeros(V), where=outdeg > 0)
         r = (1.0 - 0.85) / V + 0.85 * (A.T @ contrib)
     assert rel_l1(oracle.pagerank(off, dst, 20, 0.85), r) < 1e-12
+
+
+# ------------------------------------------------- the reference's own apps
+@pytest.mark.parametrize("name", ["rmat10_k16_sym", "rmat11_k8_dir", "grid32"])
+def test_oracle_matches_the_reference_apps(app_golden, name):
+    """tests/golden/ref_apps.npz holds what easy_graphit's apps/{pr,cc,bc,bfs,
+    sssp}.cpp compute when they run on the CPU (their UDFs, loops and constants;
+    float vertex data in double): the oracle's restatements give the same
+    values -- PageRank and BC to rounding, the integer apps exactly."""
+    from tests.conftest import app_graph
+    off, dst, w = app_graph(app_golden, name)
+    srcs = [int(s) for s in app_golden[f"sources/{name}"]]
+    # pr.cpp: damp is a float constant (0.85f), used in double here as there
+    pr = oracle.pagerank(off, dst, 20, float(np.float32(0.85)))
+    assert rel_l1(pr, app_golden[f"pr/{name}"]) <= 1e-12
+    np.testing.assert_array_equal(oracle.cc(off, dst), app_golden[f"cc/{name}"])
+    for k, s in enumerate(srcs):
+        assert rel_l1(oracle.bc(off, dst, s), app_golden[f"bc/{name}/s{k}"]) <= 1e-12, (name, s)
+    np.testing.assert_array_equal(oracle.bfs(off, dst, srcs[0]), app_golden[f"bfs/{name}"])
+    for d in (1, 8, 32):
+        want = app_golden[f"sssp/{name}/d{d}"]
+        np.testing.assert_array_equal(oracle.sssp_dijkstra(off, dst, w, srcs[0]), want)
+
+
+def test_reference_app_golden_is_not_trivial(app_golden):
+    """The fixtures exercise the apps: reached sets are large, BC has nonzero
+    dependencies, CC finds components, PageRank sums to about one."""
+    for name in ["rmat10_k16_sym", "rmat11_k8_dir", "grid32"]:
+        assert (app_golden[f"bfs/{name}"] > 1).sum() > 100
+        assert (app_golden[f"sssp/{name}/d8"] != INT_MAX).sum() > 100
+        assert np.abs(app_golden[f"bc/{name}/s0"]).sum() > 0
+        assert 0.5 < app_golden[f"pr/{name}"].sum() <= 1.0 + 1e-9
+    assert len(np.unique(app_golden["cc/rmat11_k8_dir"])) > 1
+
+
+def test_reference_apps_reproduce_the_golden(app_golden, tmp_path):
+    """Where the reference apps were built here (oracle/_ref/app_*, made from
+    the reference tree by `make -C oracle apps`), running them again on the
+    grid reproduces the stored outputs exactly."""
+    from pathlib import Path
+
+    from tests.conftest import app_graph
+    ref = Path(oracle.__file__).resolve().parent / "_ref"
+    if not all((ref / f"app_{a}").exists() for a in ("pr", "cc", "bc", "bfs", "sssp")):
+        pytest.skip("reference apps not built here (they need the reference tree)")
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "make_app_golden", Path(__file__).resolve().parent / "golden" / "make_app_golden.py")
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    off, dst, w = app_graph(app_golden, "grid32")
+    gf = str(tmp_path / "grid32.graphit_bin")
+    mk.write_graphit_bin(gf, off, dst, w)
+    s = int(app_golden["sources/grid32"][0])
+    np.testing.assert_array_equal(mk.run_app("pr", gf)["old_rank"], app_golden["pr/grid32"])
+    np.testing.assert_array_equal(mk.run_app("cc", gf)["ID"], app_golden["cc/grid32"])
+    np.testing.assert_array_equal(mk.run_app("bc", gf, s, 0.0)["dependences"], app_golden["bc/grid32/s0"])
+    np.testing.assert_array_equal(mk.run_app("sssp", gf, s, 8)["SP"], app_golden["sssp/grid32/d8"])
+    parent = mk.run_app("bfs", gf, s, 0.0)["parent"]
+    np.testing.assert_array_equal(mk.depths_from_parents(parent, s), app_golden["bfs/grid32"])
