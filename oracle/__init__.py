@@ -2,7 +2,9 @@
 
 ctypes wrapper of oracle/liboracle.so (the CPU restatement in oracle.cpp) and
 of the reference-built checker oracle/_ref/ref_gapbs (ref_gapbs.cpp compiled
-against the reference's GAPBS headers).  Only tests/, __graft_entry__.smoke()
+against the reference's GAPBS headers).  The reference's own apps, compiled
+against oracle/app_shim into oracle/_ref/app_*, are run by
+tests/golden/make_app_golden.py.  Only tests/, __graft_entry__.smoke()
 and bench.py's CPU-baseline legs use this package; the engine never does.
 """
 from __future__ import annotations

@@ -9,9 +9,11 @@
 // fixtures produced by the reference's own code compiled here (oracle/_ref,
 // built from runtime/infra_gapbs by oracle/Makefile): GAPBS-built graphs and
 // GAPBS's OrderedProcessingOperatorNoMerge SSSP distances, weighted and with
-// unit weights (= BFS depths).  The SSSP and BFS functions below are checked
-// against those; PR, CC and BC have no reference CPU code and are pinned by
-// hand-computed known answers on tiny graphs (tests/test_oracle.py).
+// unit weights (= BFS depths), and the outputs of the reference's five apps
+// themselves (apps/*.cpp compiled against oracle/app_shim, a host-execution
+// stand-in for the absent BuildIt staging library, by `make -C oracle apps`).
+// Every function below is checked against those (tests/test_oracle.py), besides
+// hand-computed known answers on tiny graphs.
 #include <algorithm>
 #include <atomic>
 #include <climits>
