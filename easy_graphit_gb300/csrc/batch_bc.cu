@@ -44,7 +44,8 @@ struct BcState {
   int64_t *work;                 // (v << 32 | chunk)
   int32_t wcap;
   int32_t chunk;                 // in-edges per work item (the graph's batch tuning)
-  int32_t *ctr;                  // [0] level-list end, [1..2] forward items, [3..4] backward items
+  int32_t *ctr;                  // [0] level-list end, [1..2] forward items, [3..4] backward items,
+                                 // [16..19] hand-out counters, [20] end of Q_0
   uint16_t *depth;               // [V][64]
   double *sigma, *dep;           // [V][64]
   const int32_t *toff, *tsrc;    // in-neighbours (the CSR itself for a symmetric graph)
@@ -165,9 +166,18 @@ __global__ void __launch_bounds__(512) k_bc_batch(DGraph g, BcState st) {
   bool alive = true;
   int32_t d = 0;
   int32_t b_prev = 0, b_d = 0;  // starts of Q_{d-1} and Q_d in the level list
+  // End of Q_d in the level list.  Not read from the list's append counter at
+  // the top of an iteration: a CTA that is ahead may already be appending
+  // Q_{d+1} there while another still reads it, and CTAs that disagree on a
+  // level's end disagree on when the loop ends (one leaves, the others wait at
+  // the next grid barrier).  Q_0's end comes from a word the seed kernel wrote
+  // and nothing appends to; each later one from the publish phase, which reads
+  // the counter between the barrier that ends the appends and the one after
+  // which the next level's appends begin.
+  int32_t e_next = *(volatile int32_t *)(st.ctr + 20);
   // ------------------------------------------------------------- forward
   for (;; ++d) {
-    const int32_t e_d = *(volatile int32_t *)(st.ctr + 0);
+    const int32_t e_d = e_next;
     if (e_d == b_d) break;  // Q_d is empty
     if (stopped(st.stop, st.err)) {
       alive = false;
@@ -233,7 +243,7 @@ __global__ void __launch_bounds__(512) k_bc_batch(DGraph g, BcState st) {
     }
     // publish Q_{d+1}: masks, depths, and its sigma work items
     {
-      const int32_t e_next = min(*(volatile int32_t *)(st.ctr + 0), st.levcap);
+      e_next = min(*(volatile int32_t *)(st.ctr + 0), st.levcap);
       const int32_t m = e_next - e_d;
       const int32_t m_up = (m + 31) & ~31;
       uint64_t *nm = bc_fr(st, d + 1);
@@ -353,6 +363,7 @@ __global__ void k_bcb_seed(BcState st, const int32_t *__restrict__ srcs) {
     st.sigma[(int64_t)v * kBcWidth + s] = 1.0;
   }
   st.ctr[0] = n;
+  st.ctr[20] = n;  // Q_0's end, read by every CTA before any appends to ctr[0]
   *st.stop = 0;
 }
 

@@ -223,22 +223,25 @@ __device__ __forceinline__ void mesh_park(const MeshView &mv, const MeshSink &s,
 }
 
 // Relaxes the out-edges [b, e) of v, kMeshInFlight edges at a time: their
-// targets and weights, loaded with v's current distance, which replaces the
-// entry's priority p when it is lower (v was lowered after it was listed; a
-// lowering within the same bucket finds v listed there already and adds no
-// entry).  A vertex now below the window was relaxed in an earlier window at
-// that value and stops here.  Then the targets' distances, stamps and edge
+// targets and weights -- for a ring entry (`check`) loaded with v's current
+// distance, which replaces the entry's priority p when it is lower (v was
+// lowered after it was listed; a lowering within the same bucket finds v
+// listed there already and adds no entry), and a vertex now below the window
+// was relaxed in an earlier window at that value and stops here.  Any other
+// entry carries a value that was current when it was listed, and a later
+// lowering listed the vertex again, so it needs no such load.  Then the
+// targets' distances, stamps and edge
 // ranges, then fire-and-forget minima for the improving ones (an improvement
 // is decided against the value read: redundant at worst, never lost).
 // Improvements below the cutoff go to the next relax list, the others park;
 // both carry the target's edge range, so neither needs a load before its own
 // relax.
 __device__ __forceinline__ void mesh_relax(const MeshView &mv, const MeshSink &s, int32_t v, int32_t p, int32_t b,
-                                           int32_t e, int32_t &smin) {
+                                           int32_t e, bool check, int32_t &smin) {
   for (int32_t k0 = b; k0 < e; k0 += kMeshInFlight) {
     int32_t d[kMeshInFlight], np[kMeshInFlight], prev[kMeshInFlight], st[kMeshInFlight];
     int32_t db[kMeshInFlight], de[kMeshInFlight];
-    const int32_t now = k0 == b ? __ldcg(mv.dist + v) : p;  // issued with the edges below
+    const int32_t now = check && k0 == b ? __ldcg(mv.dist + v) : p;  // issued with the edges below
 #pragma unroll
     for (int j = 0; j < kMeshInFlight; ++j) {
       const int32_t k = k0 + j;
@@ -285,8 +288,8 @@ __device__ __forceinline__ void mesh_fold_add(int32_t v, int32_t *dst) {
 }
 
 // A ring slot's entries all belong to its bucket: every one goes to the relax
-// list as it is (an entry whose vertex has been lowered since stops in
-// mesh_relax).
+// list as it is, its end edge stored as ~e to mark it as a ring entry, whose
+// relax reads the vertex's current distance (mesh_relax).
 __device__ __forceinline__ void mesh_scan_slot(const MeshView &mv, const MeshSink &s, const int4 *__restrict__ slot,
                                                int32_t n) {
   for (int32_t i0 = threadIdx.x; i0 < n; i0 += kMeshInFlight * blockDim.x) {
@@ -296,7 +299,7 @@ __device__ __forceinline__ void mesh_scan_slot(const MeshView &mv, const MeshSin
       x[j] = i0 + j * (int32_t)blockDim.x < n ? __ldcg(slot + i0 + j * blockDim.x) : make_int4(-1, 0, 0, 0);
 #pragma unroll
     for (int j = 0; j < kMeshInFlight; ++j)
-      if (x[j].x >= 0) mesh_list_push(mv, s, x[j].x, x[j].y, x[j].z, x[j].w);
+      if (x[j].x >= 0) mesh_list_push(mv, s, x[j].x, x[j].y, x[j].z, ~x[j].w);
   }
 }
 
@@ -555,7 +558,7 @@ __global__ void __launch_bounds__(kMeshThreads) k_sssp_cta(CtaSsspArgs c) {
       for (int32_t i = threadIdx.x; i < nq; i += blockDim.x) {
         const int32_t v = __ldcg(q + i);
         const int32_t p = __ldcg(mv.dist + v), b = __ldg(mv.off + v), e = __ldg(mv.off + v + 1);
-        mesh_relax(mv, s, v, p, b, e, smin);
+        mesh_relax(mv, s, v, p, b, e, false, smin);
       }
     } else {
       // an advance to the window [nJ delta, win): the bucket's ring slot and the
@@ -571,7 +574,7 @@ __global__ void __launch_bounds__(kMeshThreads) k_sssp_cta(CtaSsspArgs c) {
         if (ns > T) mesh_scan_slot(mv, s, slot + T, ns - T);
         if ((int32_t)threadIdx.x < ns) {
           const int4 x = __ldcg(slot + threadIdx.x);
-          mesh_relax(mv, s, x.x, x.y, x.z, x.w, smin);
+          mesh_relax(mv, s, x.x, x.y, x.z, x.w, true, smin);
         }
         if (C.nsp > 0) {
           int32_t nd = 0;
@@ -605,7 +608,7 @@ __global__ void __launch_bounds__(kMeshThreads) k_sssp_cta(CtaSsspArgs c) {
       s.list_cnt = &C.list_cnt[r % 3];
       for (int32_t i = threadIdx.x; i < nl; i += blockDim.x) {
         const int4 x = lin[i];
-        mesh_relax(mv, s, x.x, x.y, x.z, x.w, smin);
+        mesh_relax(mv, s, x.x, x.y, x.z, x.w < 0 ? ~x.w : x.w, x.w < 0, smin);
       }
       mesh_fold_min(smin, &C.srec);
       smin = INT_MAX;
