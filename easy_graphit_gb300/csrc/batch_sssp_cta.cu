@@ -151,9 +151,10 @@ struct MeshSink {
   int32_t *far, *far_cnt;   // far pile the step appends to
   int32_t far_tag;
   int32_t *sp, *sp_cnt;     // spill pile (ring slots that are full)
-  int4 *list;               // relax list of this round (v, p, b, e); b < 0: edges not loaded
+  int4 *list;               // relax list of this round (v, p, b, e); e < 0: a ring entry, end edge ~e
   int32_t *list_cnt;
   int32_t *q, *q_cnt;       // overflow queue of this step
+  int32_t qtag;             // stamp of a vertex on that queue (below every pile tag)
 };
 
 __device__ __forceinline__ int32_t mesh_far_tag(int32_t gen) { return -gen - 1; }
@@ -182,14 +183,18 @@ __device__ __forceinline__ void mesh_ring_append(const MeshView &mv, const MeshS
   }
 }
 
-// v (at priority p, edges [b, e)) goes to the relax list; a full list spills
-// v to the overflow queue, whose step re-reads its distance and edges.
+// v (at priority p, edges [b, e)) goes to the relax list; a full list sends v
+// to the step's overflow queue, whose step re-reads its distance and edges.
+// The queue takes a vertex once per step (its stamp exchanged for the step's
+// tag), so it never holds more than V entries; a stamp taken over this way
+// only lets a later park list the vertex again (a duplicate, never a miss).
 __device__ __forceinline__ void mesh_list_push(const MeshView &mv, const MeshSink &s, int32_t v, int32_t p,
                                                int32_t b, int32_t e) {
   const int32_t pos = agg_inc(s.list_cnt);
   if (pos < kMeshList) {
     s.list[pos] = make_int4(v, p, b, e);
   } else {
+    if (atomicExch(mv.stamp + v, s.qtag) == s.qtag) return;
     const int32_t qp = agg_inc(s.q_cnt);
     if (qp < mv.qcap)
       s.q[qp] = v;
@@ -520,6 +525,7 @@ __global__ void __launch_bounds__(kMeshThreads) k_sssp_cta(CtaSsspArgs c) {
     s.list_cnt = &C.list_cnt[0];
     s.q = in ? mv.q[0] : mv.q[1];
     s.q_cnt = &C.q_cnt[in ^ 1];
+    s.qtag = INT_MIN + 1 + (C.steps & 0x3fffffff);
     int32_t smin = INT_MAX;  // smallest value this thread left on a spill pile
     if (kind == MESH_HIMIN) {
       // smallest live value of the far pile (everything at or above the cutoff)

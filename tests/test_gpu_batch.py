@@ -355,3 +355,25 @@ def test_sssp_batch_light_and_heavy_edges(delta):
         np.testing.assert_array_equal(dist[i], oracle.sssp_dijkstra(off, dst, ww, int(s)),
                                       err_msg=f"source {s}")
     g.close()
+
+
+@pytest.mark.parametrize("delta", [1, 32, 1000])
+def test_sssp_one_cta_per_source_forced_on_a_graph_with_hubs(delta):
+    """The per-source form (one CTA per source, bucket ring) forced onto a
+    directed R-MAT 12 (hubs of hundreds of edges; at delta 1000 one window
+    holds most of the graph): ring slots fill and spill, relax lists overflow
+    into the per-step queue, edge ranges exceed a group of four -- the
+    distances still equal Dijkstra's, and equal the lane-per-source kernel's."""
+    from easy_graphit_gb300 import set_batch_tuning
+    hg = HostGraph.rmat(12, 16)
+    g = GraphT(hg)
+    off, dst, w = np.array(hg.offsets), np.array(hg.dst), np.array(hg.weights)
+    srcs = hg.pick_sources(8, seed=5)
+    set_batch_tuning(g, "sssp", per_source_cta=1)
+    cta, _ = sssp_batch(g, srcs, delta)
+    set_batch_tuning(g, "sssp", per_source_cta=-1)
+    lane, _ = sssp_batch(g, srcs, delta)
+    np.testing.assert_array_equal(cta, lane)
+    for i, s in enumerate(srcs):
+        np.testing.assert_array_equal(cta[i], oracle.sssp_dijkstra(off, dst, w, int(s)), err_msg=f"source {s}")
+    g.close()
