@@ -1,7 +1,7 @@
 // Batched SSSP for high-diameter graphs: every source gets a CTA of its own,
 // which runs the whole delta-stepping loop for that source alone -- its
-// distance row, stamps, far piles and overflow queues private to it, its
-// control words and relax lists in shared memory, __syncthreads between
+// distance row, stamps, piles, ring and queues private to it, its control
+// words and relax lists in shared memory, __syncthreads between
 // steps and no grid barrier at all.  The CTAs of a pass run side by side, one
 // source each.
 //
@@ -13,29 +13,28 @@
 // and one CTA per source is too little parallelism: the lane-per-source
 // kernel stays the choice there (gg_batch_tuning.per_source_cta).
 //
-// The loop keeps the delta-stepping rule of gpu_priority_queue.h (the window
-// [cur, cur+delta) is relaxed until nothing in it improves, then the next
-// window starts at the smallest pending priority) with the far piles of
-// bucket_queue.cuh, re-arranged so that a bucket costs one step:
-//  - an advance scans the low pile and relaxes the window's vertices in the
-//    same step: window entries go to a relax list in shared memory (with the
-//    distance and edge range the scan loaded), and the relax runs as soon as
-//    the scan is done;
-//  - improvements inside the window go to the other shared list and are
-//    relaxed in further rounds of the same step (one __syncthreads a round),
-//    not in later steps through a global queue (a list that fills up spills
-//    to one, which the next step relaxes);
-//  - the low pile is scanned in place: live entries stay where they are and
-//    their values are folded into the minimum that starts the next window
-//    (never above the smallest pending priority; if the vertex that set it
-//    was lowered since, the window comes out empty and the next advance starts
-//    from the values folded meanwhile); a pile whose entries are mostly dead
-//    is compacted into a new generation by the next advance;
-//  - parks check the vertex's stamp, loaded with its distance, before they
-//    exchange it.
-// Results are each source's exact distances; the bucket boundaries may start
-// below the reference's (an early window holds fewer vertices), which changes
-// the number of advances, never a distance.
+// The loop is delta-stepping with windows [J delta, (J+1) delta) (the window
+// is relaxed until nothing in it improves, then the next nonempty bucket
+// opens), over a structure shaped so that a bucket costs one step:
+//  - a ring of kMeshSlots buckets ahead of the current one, each a list of
+//    whole entries (vertex, priority, first edge, end edge): a relaxation
+//    that lowers a vertex to a later bucket lists it in that bucket's slot
+//    (stamp[v] = J + 1 keeps it listed once per bucket), so an advance takes
+//    the next nonempty slot without scanning anything else, and the entry
+//    carries what its relax needs (parks load the target's edge range with its
+//    distance);
+//  - buckets beyond the ring go to a far pile, split into a new ring when the
+//    ring runs dry (its smallest live value opens the next window); a full
+//    slot spills to a pile that every advance scans in place (compacted when
+//    mostly dead);
+//  - the thread that reads a slot entry relaxes it; improvements inside the
+//    window go to a shared-memory list and are relaxed in further rounds of
+//    the same step (one __syncthreads a round); a full list sends vertices to
+//    a per-step queue that the next step relaxes;
+//  - warp 0 closes a step and decides the next one in one pass.
+// Results are each source's exact distances.  The windows are aligned to
+// multiples of delta where the reference's start at the exact minimum, which
+// changes the number of advances, never a distance.
 #include <atomic>
 #include <vector>
 
@@ -101,7 +100,7 @@ __host__ __device__ __forceinline__ int64_t mesh_block_ints(int64_t n) {
 enum : int32_t { MESH_RELAX = 0, MESH_ADV = 1, MESH_HIMIN = 2, MESH_HISPLIT = 3, MESH_COMPACT = 4, MESH_DONE = 5 };
 
 // Shared control words of one source's loop.  Counters are appended to during
-// a step; the state below them is written by thread 0 between steps.
+// a step; the state below them is written by warp 0 between steps.
 struct MeshCtl {
   int32_t rc[kMeshSlots];  // entries of each ring slot
   int32_t far_cnt[2];      // far piles, by generation parity
