@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(512) k_bc_batch(DGraph g, BcState st) {
   for (;; ++d) {
     const int32_t e_d = e_next;
     if (e_d == b_d) break;  // Q_d is empty
-    if (stopped(st.stop, st.err)) {
+    if (stopped(st.stop, d)) {
       alive = false;
       break;
     }
@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(512) k_bc_batch(DGraph g, BcState st) {
         bc_push_items(st, st.ctr + 1 + (d & 1), v, nch);
       }
     }
-    clk.tick(st.stop);
+    clk.tick(st.stop, d, st.err);
     if (!grid_barrier(st.bar, gridDim.x, st.err, st.timeout_ns)) {
       alive = false;
       break;
@@ -275,8 +275,9 @@ __global__ void __launch_bounds__(512) k_bc_batch(DGraph g, BcState st) {
   const int32_t L = d;  // levels 0 .. L-1 are non-empty
   if (tid == 0) st.stats[0] = L;
   // ------------------------------------------------------------ backward
-  for (int32_t dd = L - 1; alive && dd >= 0; --dd) {
-    if (stopped(st.stop, st.err)) break;
+  // (iterations numbered on from the forward loop's, for the loop clock)
+  for (int32_t dd = L - 1, it = L + 1; alive && dd >= 0; --dd, ++it) {
+    if (stopped(st.stop, it)) break;
     if (tid == 0) {
       st.ctr[3 + ((dd + 1) & 1)] = 0;   // consumed by the gather of level dd + 1
       st.ctr[18 + ((dd + 1) & 1)] = 0;  // that gather's hand-out counter
@@ -345,7 +346,7 @@ __global__ void __launch_bounds__(512) k_bc_batch(DGraph g, BcState st) {
         }
       }
     }
-    clk.tick(st.stop);
+    clk.tick(st.stop, it, st.err);
     if (!grid_barrier(st.bar, gridDim.x, st.err, st.timeout_ns)) break;
   }
 }

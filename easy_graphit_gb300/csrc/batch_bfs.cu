@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(512) k_msbfs(DGraph g, MsBfsState st) {
   double vis_v = 0, vis_e = 0;  // running totals of the frontiers so far (the same in every CTA)
   for (;; ++L) {
     const int32_t n = *(volatile int32_t *)(st.cnt4 + (L & 3));
-    if (n == 0 || stopped(st.stop, st.err)) break;
+    if (n == 0 || stopped(st.stop, L)) break;
     const volatile unsigned long long *ls = st.lstat + 4 * (L % 3);
     const double sd = (double)ls[0], sd2 = (double)ls[1], mx = (double)ls[2];
     if (tid == 0) {
@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(512) k_msbfs(DGraph g, MsBfsState st) {
         atomicMax(nx + 2, s_stat[2]);
       }
     }
-    clk.tick(st.stop);
+    clk.tick(st.stop, L, st.err);
     if (!grid_barrier(st.bar, gridDim.x, st.err, st.timeout_ns)) break;
   }
   if (tid == 0) {

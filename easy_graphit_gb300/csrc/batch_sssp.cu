@@ -470,7 +470,7 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
   LoopClock clk;
   clk.start(S.loop_limit_ns);
   for (;; ++it) {
-    if (stopped(S.stop, S.err)) break;
+    if (stopped(S.stop, it)) break;
     const int32_t n = *(volatile int32_t *)(S.cnt + (it - 1) % 3);
     int32_t *qcnt_out = S.cnt + it % 3;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -554,7 +554,7 @@ __global__ void __launch_bounds__(256, 4) k_bsssp(BsState S) {
       act = __reduce_or_sync(kFull, act);
       if (lane == 0 && act) atomicOr(reinterpret_cast<uint32_t *>(S.cnt + 5 + it % 3), act);
     }
-    clk.tick(S.stop);
+    clk.tick(S.stop, it, S.err);
     if (!grid_barrier(S.bar, gridDim.x, S.err, S.timeout_ns)) break;
     // ---- advance the sources with no near work
     uint32_t unfinished = 0;

@@ -257,22 +257,32 @@ __device__ __forceinline__ bool grid_wait_others(const uint32_t *bar, uint32_t n
   return ok_o != 0;
 }
 
-// Wall-clock bound of a persistent loop.  Block 0 raises *stop just before an
-// iteration's closing grid barrier, so every block reads the same value at the
-// top of the next iteration and all leave together (DEV_ERR_TIMEOUT recorded).
+// Wall-clock bound of a persistent loop.  In iteration `iter`, just before its
+// closing grid barrier, block 0 checks the clock and, the first time it has
+// passed, records DEV_ERR_TIMEOUT and writes iter + 1 into *stop: the number
+// of the iteration at whose top every block leaves.  A number rather than a
+// flag: a block that reads *stop late at the top of iteration `iter` (block 0
+// may already be past that point) sees iter + 1 and goes on, so all blocks
+// still leave together at the top of iteration iter + 1.
 struct LoopClock {
   uint64_t deadline;
   __device__ __forceinline__ void start(uint64_t limit_ns) { deadline = globaltimer_ns() + limit_ns; }
-  __device__ __forceinline__ void tick(int32_t *stop) const {
-    if (blockIdx.x == 0 && threadIdx.x == 0 && globaltimer_ns() > deadline) atomicExch(stop, 1);
+  __device__ __forceinline__ void tick(int32_t *stop, int32_t iter, int32_t *err) const {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && globaltimer_ns() > deadline &&
+        atomicCAS(stop, 0, iter + 1) == 0)
+      atomicOr(err, DEV_ERR_TIMEOUT);
   }
 };
-__device__ __forceinline__ bool stopped(const int32_t *stop, int32_t *err) {
-  if (*(volatile const int32_t *)stop) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, DEV_ERR_TIMEOUT);
-    return true;
-  }
-  return false;
+// True at the top of iteration `iter` once a stop has been set for it.
+__device__ __forceinline__ bool stopped(const int32_t *stop, int32_t iter) {
+  const int32_t s = *(volatile const int32_t *)stop;
+  return s != 0 && iter >= s;
+}
+// The same stop for a reason other than the clock (block 0, before the
+// iteration's closing barrier): a sparse queue that overflowed.
+__device__ __forceinline__ void stop_on_overflow(int32_t *stop, int32_t iter, const int32_t *err) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (*(volatile const int32_t *)err & DEV_ERR_OVERFLOW))
+    atomicCAS(stop, 0, iter + 1);
 }
 
 __host__ __device__ __forceinline__ int32_t ceil_div(int64_t a, int64_t b) {

@@ -87,13 +87,13 @@ __global__ void __launch_bounds__(1024) k_bfs_fused(FusedArgs a) {
   clk.start(a.loop_limit_ns);
   for (;; ++level) {
     const int32_t n = *(volatile int32_t *)(a.cnt3 + (level - 1) % 3);
-    if (n == 0 || stopped(a.stop, a.err)) break;
+    if (n == 0 || stopped(a.stop, (int32_t)level)) break;
     if (blockIdx.x == 0 && threadIdx.x == 0) a.cnt3[(level + 1) % 3] = 0;
     const Enum en{qs[in], nullptr, n};
     const EdgeF<UBfs, false> f{UBfs{a.vd.parent, a.vd.depth, (int32_t)level},
                                DIn{IN_ALL, nullptr, nullptr}, DIn{IN_ALL, nullptr, nullptr}, true};
     run_lb<LB>(a.g, en, n, f, sparse_out(a, qs[in ^ 1], level), smem, blockIdx.x, gridDim.x);
-    clk.tick(a.stop);
+    clk.tick(a.stop, (int32_t)level, a.err);
     if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
     in ^= 1;
   }
@@ -161,8 +161,10 @@ __global__ void __launch_bounds__(1024) k_sssp_bq(BqArgs a) {
   int32_t *stop = a.b.ctl + BQ_STOP;
   LoopClock clk;
   clk.start(a.loop_limit_ns);
-  for (;;) {
-    if (stopped(stop, a.err) || (*(volatile int32_t *)a.err & (DEV_ERR_OVERFLOW | DEV_ERR_TIMEOUT))) break;
+  // Grid iterations (one barrier each), numbered for the stop word: the clock
+  // and a flagged overflow stop every block at the top of the same iteration.
+  for (int32_t round = 0;; ++round) {
+    if (stopped(stop, round)) break;
     const BqStep st = bq_decide(s, a.b.ctl, a.delta);
     if (st.kind == BQ_DONE) {
       if (s.phase == 0) s.adv++;  // the reference's last advance finds no priority left
@@ -177,7 +179,8 @@ __global__ void __launch_bounds__(1024) k_sssp_bq(BqArgs a) {
         else
           bq_publish(s, a.b.ctl);
       }
-      clk.tick(stop);
+      clk.tick(stop, round, a.err);
+      stop_on_overflow(stop, round, a.err);
       if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
       const volatile int32_t *pub = a.b.ctl + BQ_PUB;
       int32_t *p = reinterpret_cast<int32_t *>(&s);
@@ -185,7 +188,8 @@ __global__ void __launch_bounds__(1024) k_sssp_bq(BqArgs a) {
       continue;
     }
     bq_step<LB>(s, a, st, a.b.ctl, blockIdx.x, gridDim.x, smem, red);
-    clk.tick(stop);
+    clk.tick(stop, round, a.err);
+    stop_on_overflow(stop, round, a.err);
     if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -406,7 +410,7 @@ __global__ void __launch_bounds__(kBfsDoMaxCta, 4) k_bfs_do(DoKernelArgs ka, uin
     unsigned long long r = 0ull;
     if (d.stats && threadIdx.x < 3) r = *(volatile unsigned long long *)(d.lstat + 4 * ((level - 1) % 3) + threadIdx.x);
     const int32_t n = *(volatile int32_t *)(a.cnt3 + (level - 1) % 3);
-    if (n == 0 || stopped(a.stop, a.err)) break;
+    if (n == 0 || stopped(a.stop, level)) break;
     const bool logged = d.feat_log && level - 1 <= d.max_log;
     // The level's direction, decided by warp 0 alone (statistics, features,
     // network) and handed to the CTA by one barrier.
@@ -493,7 +497,7 @@ __global__ void __launch_bounds__(kBfsDoMaxCta, 4) k_bfs_do(DoKernelArgs ka, uin
         atomicMax(nx + 2, (unsigned long long)s_stat.mx);
       }
     }
-    clk.tick(a.stop);
+    clk.tick(a.stop, level, a.err);
     if (!grid_barrier(a.bar, gridDim.x, a.err, a.timeout_ns)) break;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
