@@ -248,19 +248,31 @@ struct VertexData {
   }
 };
 
-// gpu_priority_queue.h:33-153 and 250-297 run sequentially.
+// gpu_priority_queue.h:33-153 and 250-297 run sequentially.  The number of
+// window moves of the last run (each a scan for the next priority, the last
+// one finding none) is written out as <name>_advances.
 struct PriorityQueue {
   VertexData<int> *p = nullptr;
   long long current = 0, window_upper = 0, cutoff = 0;
   int delta = 1;
   bool ready = false;
+  int advances = 0;
   std::vector<int> frontier, out;
-  explicit PriorityQueue(std::string) {}
+  explicit PriorityQueue(std::string name) {
+    registry().push_back({name, [this, name](const std::string &dir) {
+                            const std::string path = dir + "/" + name + "_advances.i32";
+                            FILE *f = std::fopen(path.c_str(), "wb");
+                            if (!f) std::exit(1);
+                            std::fwrite(&advances, sizeof(int), 1, f);
+                            std::fclose(f);
+                          }});
+  }
   void init(GraphT &, VertexData<int> &p_, int init_p, int delta_, int src = -1) {
     p = &p_;
     current = init_p;
     delta = delta_;
     ready = false;
+    advances = 0;
     frontier.clear();
     if (src != -1) frontier.push_back(src);
     cutoff = current + delta;
@@ -273,6 +285,7 @@ struct PriorityQueue {
     }
   }
   void advance() {
+    ++advances;
     window_upper = current + delta;
     long long m = INT_MAX;
     for (int x : p->data)

@@ -11,7 +11,9 @@ in double there, so PageRank and BC come out in FP64.  Stored per graph g:
   * cc/<g>: ID;
   * bc/<g>/s<k>: dependences from sources/<g>[k];
   * bfs/<g>: hop depths along the app's parent tree from sources/<g>[0] (-1 unreached);
-  * sssp/<g>/d<delta>: SP from sources/<g>[0] (INT_MAX unreached);
+  * sssp/<g>/d<delta>: SP from sources/<g>[0] (INT_MAX unreached), and
+    sssp/<g>/adv<delta>: how many times the app's priority queue moved its
+    window (the count the engine's single-source queues are held to);
   * how to rebuild g: graph/<g>/{scale,degree,symmetrize,sha256} for the R-MAT
     graphs (oracle.rmat, itself pinned to the reference's builder), the full
     CSR graph/<g>/{offsets,dst,w} for the grid.
@@ -147,7 +149,9 @@ def main() -> None:
                 out[f"bc/{name}/s{k}"] = run_app("bc", gf, s, 0.0)["dependences"]
             out[f"bfs/{name}"] = depths_from_parents(run_app("bfs", gf, srcs[0], 0.0)["parent"], srcs[0])
             for d in DELTAS:
-                out[f"sssp/{name}/d{d}"] = run_app("sssp", gf, srcs[0], d)["SP"]
+                r = run_app("sssp", gf, srcs[0], d)
+                out[f"sssp/{name}/d{d}"] = r["SP"]
+                out[f"sssp/{name}/adv{d}"] = r["pq_advances"]
     path = Path(__file__).with_name("ref_apps.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({path.stat().st_size} bytes, {len(out)} arrays)")

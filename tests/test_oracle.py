@@ -229,6 +229,10 @@ def test_oracle_matches_the_reference_apps(app_golden, name):
     for d in (1, 8, 32):
         want = app_golden[f"sssp/{name}/d{d}"]
         np.testing.assert_array_equal(oracle.sssp_dijkstra(off, dst, w, srcs[0]), want)
+        # the bucket rule: as many window moves as sssp.cpp's own loop makes
+        dist, adv = oracle.sssp_delta_gpu(off, dst, w, srcs[0], d)
+        np.testing.assert_array_equal(dist, want)
+        assert adv == int(app_golden[f"sssp/{name}/adv{d}"][0]), (name, d)
 
 
 def test_reference_app_golden_is_not_trivial(app_golden):
