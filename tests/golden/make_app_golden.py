@@ -14,6 +14,8 @@ in double there, so PageRank and BC come out in FP64.  Stored per graph g:
   * sssp/<g>/d<delta>: SP from sources/<g>[0] (INT_MAX unreached), and
     sssp/<g>/adv<delta>: how many times the app's priority queue moved its
     window (the count the engine's single-source queues are held to);
+  * config1/depth: bfs.cpp's hop depths on the symmetrized R-MAT 16 (edge
+    factor 16) from its highest-degree vertex (config1/source, config1/sha256);
   * how to rebuild g: graph/<g>/{scale,degree,symmetrize,sha256} for the R-MAT
     graphs (oracle.rmat, itself pinned to the reference's builder), the full
     CSR graph/<g>/{offsets,dst,w} for the grid.
@@ -152,6 +154,14 @@ def main() -> None:
                 r = run_app("sssp", gf, srcs[0], d)
                 out[f"sssp/{name}/d{d}"] = r["SP"]
                 out[f"sssp/{name}/adv{d}"] = r["pq_advances"]
+        # the BFS workload as stated: symmetrized R-MAT 16, highest-degree source
+        off, dst, w = (np.asarray(a) for a in oracle.rmat(16, 16, symmetrize=True))
+        gf = os.path.join(tmp, "config1.graphit_bin")
+        write_graphit_bin(gf, off, dst, w)
+        src = int(np.argmax(np.diff(off)))
+        out["config1/source"] = np.array(src, dtype=np.int32)
+        out["config1/sha256"] = np.array(digest(off, dst, w))
+        out["config1/depth"] = depths_from_parents(run_app("bfs", gf, src, 0.0)["parent"], src)
     path = Path(__file__).with_name("ref_apps.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({path.stat().st_size} bytes, {len(out)} arrays)")

@@ -271,3 +271,18 @@ def test_reference_apps_reproduce_the_golden(app_golden, tmp_path):
     np.testing.assert_array_equal(mk.run_app("sssp", gf, s, 8)["SP"], app_golden["sssp/grid32/d8"])
     parent = mk.run_app("bfs", gf, s, 0.0)["parent"]
     np.testing.assert_array_equal(mk.depths_from_parents(parent, s), app_golden["bfs/grid32"])
+
+
+def test_oracle_bfs_matches_the_reference_app_on_the_bfs_workload(app_golden):
+    """The BFS workload as stated -- symmetrized R-MAT 16, edge factor 16, from
+    its highest-degree vertex -- run by bfs.cpp itself: the oracle's depths are
+    the same, bit for bit (the GPU's are held to the oracle on this graph)."""
+    import hashlib
+    off, dst, w = (np.asarray(a, dtype=np.int32) for a in oracle.rmat(16, 16, symmetrize=True))
+    h = hashlib.sha256()
+    for a in (off, dst, w):
+        h.update(np.ascontiguousarray(a).tobytes())
+    assert h.hexdigest() == str(app_golden["config1/sha256"])
+    src = int(app_golden["config1/source"])
+    assert src == int(np.argmax(np.diff(off)))
+    np.testing.assert_array_equal(oracle.bfs(off, dst, src), app_golden["config1/depth"])
