@@ -16,6 +16,10 @@ in double there, so PageRank and BC come out in FP64.  Stored per graph g:
     window (the count the engine's single-source queues are held to);
   * config1/depth: bfs.cpp's hop depths on the symmetrized R-MAT 16 (edge
     factor 16) from its highest-degree vertex (config1/source, config1/sha256);
+  * config2/...: sssp.cpp on the directed R-MAT 22 (edge factor 16, weights
+    U[1,255]) from the first two SourcePicker sources at delta 8, 32 and 128
+    -- distances too large to store, so their SHA-256 (config2/s<k>_sha256,
+    equal at every delta) and the window moves (config2/s<k>_adv<delta>);
   * how to rebuild g: graph/<g>/{scale,degree,symmetrize,sha256} for the R-MAT
     graphs (oracle.rmat, itself pinned to the reference's builder), the full
     CSR graph/<g>/{offsets,dst,w} for the grid.
@@ -162,6 +166,22 @@ def main() -> None:
         out["config1/source"] = np.array(src, dtype=np.int32)
         out["config1/sha256"] = np.array(digest(off, dst, w))
         out["config1/depth"] = depths_from_parents(run_app("bfs", gf, src, 0.0)["parent"], src)
+        # the SSSP workload's R-MAT 22 (a few minutes: the app runs five trials
+        # and its queue scans every vertex per window move)
+        off, dst, w = (np.asarray(a) for a in oracle.rmat(22, 16))
+        gf = os.path.join(tmp, "config2.graphit_bin")
+        write_graphit_bin(gf, off, dst, w)
+        srcs = [int(x) for x in oracle.pick_sources(off, 2)]
+        out["config2/sha256"] = np.array(digest(off, dst, w))
+        out["config2/sources"] = np.array(srcs, dtype=np.int32)
+        for k, src in enumerate(srcs):
+            digests = set()
+            for d in (8, 32, 128):
+                r = run_app("sssp", gf, src, d)
+                digests.add(hashlib.sha256(np.ascontiguousarray(r["SP"], dtype=np.int32).tobytes()).hexdigest())
+                out[f"config2/s{k}_adv{d}"] = r["pq_advances"]
+            assert len(digests) == 1, "distances depend on delta"
+            out[f"config2/s{k}_sha256"] = np.array(digests.pop())
     path = Path(__file__).with_name("ref_apps.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({path.stat().st_size} bytes, {len(out)} arrays)")

@@ -286,3 +286,26 @@ def test_oracle_bfs_matches_the_reference_app_on_the_bfs_workload(app_golden):
     src = int(app_golden["config1/source"])
     assert src == int(np.argmax(np.diff(off)))
     np.testing.assert_array_equal(oracle.bfs(off, dst, src), app_golden["config1/depth"])
+
+
+def test_oracle_sssp_matches_the_reference_app_on_the_sssp_workload(app_golden):
+    """The SSSP workload's directed R-MAT 22 (weights U[1,255]) from its first
+    two SourcePicker sources, run by sssp.cpp itself at delta 8, 32, 128: the
+    oracle's Dijkstra distances hash the same, and its restatement of the
+    bucket rule makes as many window moves as the app's own queue."""
+    import hashlib
+    off, dst, w = (np.asarray(a, dtype=np.int32) for a in oracle.rmat(22, 16))
+    h = hashlib.sha256()
+    for a in (off, dst, w):
+        h.update(np.ascontiguousarray(a).tobytes())
+    assert h.hexdigest() == str(app_golden["config2/sha256"])
+    srcs = [int(x) for x in oracle.pick_sources(off, 2)]
+    assert srcs == [int(x) for x in app_golden["config2/sources"]]
+    for k, s in enumerate(srcs):
+        d = oracle.sssp_dijkstra(off, dst, w, s)
+        assert hashlib.sha256(np.ascontiguousarray(d, dtype=np.int32).tobytes()).hexdigest() == \
+            str(app_golden[f"config2/s{k}_sha256"])
+        for delta in (8, 32, 128):
+            dist, adv = oracle.sssp_delta_gpu(off, dst, w, s, delta)
+            np.testing.assert_array_equal(dist, d)
+            assert adv == int(app_golden[f"config2/s{k}_adv{delta}"][0]), (s, delta)
